@@ -1,0 +1,325 @@
+"""Benchmark: particle-substeps/s of Solver::update on GB300.
+
+Workload (N=1): the single large world of 64 cloth grids of 32x32
+(65,536 particles, 249,984 links) in a 2000^2 box with initial velocities
+N(0, 0.5), particle-particle / particle-circle / particle-polygon collisions
+on (radius 0.5, cell 1.0), 16 circles, 8 convex polygons, 8 sub-steps, 4 link
+iterations, reference-order link mode.  A step is one Solver::update(1/60).
+
+  value    device time (CUDA events on the solver's stream), inputs resident,
+           L2 flushed (256 MiB write) between timed steps
+  e2e      the same step through the C ABI with the state uploaded from and
+           downloaded to pinned host memory inside the timed region
+  roofline dominant kernel: algorithmic bytes per launch / CUDA-event time
+  cpu_baseline  the CPU oracle (port of the reference) on a bounded sample
+
+--impl reference times the CPU port of the reference on the same workload.
+Under torchrun (N>1) every rank runs its own replica (worlds are
+independent; there is no collective on the data path): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-substeps/s"
+WORKLOAD = "64 cloth grids 32x32 (65,536 particles, 249,984 links), collisions on, 8 sub-steps, 4 link iterations"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(seed: int = 0):
+    from bendy2d_gb300 import scenes
+    return scenes.config2(seed=seed)
+
+
+def algorithmic_bytes(kernel: str, sc) -> float:
+    """Algorithmic HBM bytes of one launch (per-unit figures: 32 B per
+    particle for bounds+integrate; (12 + 32) B per link per iteration for a
+    link pass: endpoints ab + rest, then read+write of both positions)."""
+    n, l = sc.n_particles, len(sc.la)
+    if kernel.startswith("exec_groups_links") or kernel == "exec_serial_links":
+        return sc.link_iters * l * 44.0
+    if kernel.startswith("exec_groups_full") or kernel == "exec_serial_full":
+        return sc.sub_steps * (sc.link_iters * l * 44.0 + 32.0 * n)
+    if kernel == "collide_integrate":
+        return 32.0 * n
+    if kernel == "grid_insert":
+        return 8.0 * n + 4.0 * n + 16.0 * n
+    return 0.0
+
+
+def run_cpu_oracle(sc, budget_s: float, max_steps: int = 1000):
+    from oracle import load_scene
+    o = load_scene(sc)
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps:
+        o.update(sc.dt)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return sc.n_particles * sc.sub_steps * steps / dt, steps, dt
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sc = build_scene()
+        warm = max(args.warmup, 0)
+        from oracle import load_scene
+        o = load_scene(sc)
+        for _ in range(min(warm, 3)):
+            o.update(sc.dt)
+        # bounded sample: at most --steps updates, and at most ~cpu-budget seconds
+        t0 = time.perf_counter()
+        k = 0
+        while k < args.steps:
+            o.update(sc.dt)
+            k += 1
+            if time.perf_counter() - t0 >= args.cpu_budget:
+                break
+        el = time.perf_counter() - t0
+        v = sc.n_particles * sc.sub_steps * k / el
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC,
+            "n_gpus": args.gpus, "steps": k, "warmup": min(warm, 3),
+            "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "parallelism": "single-threaded reference"},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"{k} updates of the full workload (C port of the "
+                                       "reference, single thread like Solver::update)"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from bendy2d_gb300 import build as b
+    b.build()
+    sc = build_scene(seed=rank)
+    stream = torch.cuda.Stream()
+    s = sc.to_solver()
+    s.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    units = sc.n_particles * sc.sub_steps
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (also builds the plan and captures the graph)
+    for _ in range(max(args.warmup, 3)):
+        s.update(sc.dt)
+    s.synchronize()
+
+    # ---- device-timed steps, state resident, L2 flushed between steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                s.update(sc.dt)
+                e1.record(stream)
+        s.synchronize()
+        barrier()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = units * args.steps * world / (ms_max / 1e3)
+    launches = s.launch_count() * args.steps
+
+    # ---- end to end through the C ABI with pinned host buffers
+    nbytes = s.state_bytes()
+    h_in = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h_out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    s.state_download_async(h_in.data_ptr())
+    s.synchronize()
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    barrier()
+    with torch.cuda.stream(stream):
+        for e0, e1 in e2e_ev:
+            flush.zero_()
+            e0.record(stream)
+            s.state_upload_async(h_in.data_ptr())
+            s.update(sc.dt)
+            s.state_download_async(h_out.data_ptr())
+            e1.record(stream)
+    s.synchronize()
+    barrier()
+    e2e_ms = sum(e0.elapsed_time(e1) for e0, e1 in e2e_ev)
+    e2e_t = torch.tensor([e2e_ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = units * args.steps * world / (float(e2e_t.item()) / 1e3)
+
+    # ---- per-kernel times (CUDA events around each launch, same stream)
+    s.set_profiling(True)
+    prof_tot = {}
+    nprof = max(3, min(args.steps, 10))
+    for _ in range(nprof):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        s.update(sc.dt)
+        for k, v in s.profile().items():
+            prof_tot[k] = prof_tot.get(k, 0.0) + v
+    s.set_profiling(False)
+    # launches of each kernel per step
+    dom = max(prof_tot, key=prof_tot.get)
+    per_step_launches = {"exec_groups_links_smem": sc.sub_steps, "collide_integrate": sc.sub_steps,
+                         "grid_insert": sc.sub_steps, "rigid_ext": sc.sub_steps + 1}
+    nl = per_step_launches.get(dom, 1)
+    dom_ms = prof_tot[dom] / nprof / nl
+    peak, peak_kind = _peaks()
+    alg = algorithmic_bytes(dom, sc)
+    achieved = alg / (dom_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(dom)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        v, k, el = run_cpu_oracle(sc, args.cpu_budget)
+        cpu = {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+               "sample": f"{k} updates of the full workload in {el:.1f} s (C port of the "
+                         "reference, single thread)"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator, bendy2d_gb300/scenes.py:config2)",
+        "config": {"workload": WORKLOAD, "particles": sc.n_particles, "links": int(len(sc.la)),
+                   "sub_steps": sc.sub_steps, "link_iters": sc.link_iters,
+                   "mode": "reference-order", "collisions": "pp+pc+ppoly",
+                   "l2": "flushed (256 MiB write) between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                     "launch_ms": dom_ms},
+        "kernel_ms_per_step": {k: v / nprof for k, v in sorted(prof_tot.items())},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

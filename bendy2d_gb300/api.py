@@ -1,0 +1,460 @@
+"""Python mirror of the reference's public API (src/lib.rs:1-6).
+
+Names, fields and meanings follow bendy2d 0.0.1: ``Solver`` (src/solver.rs),
+``Particle`` (src/particle.rs), ``Link`` / ``ParticleLink`` / ``CircleLink``
+(src/link.rs), ``Circle`` (src/circle.rs), ``Polygon`` (src/polygon.rs) and
+``Bounds`` (src/solver.rs:13-17).  Every call goes through the C ABI of
+include/bendy2d.h; ``Solver.update`` runs on the GPU.  Where the reference
+panics, the C ABI returns a status and this module raises ``B2DError``;
+where it returns ``None`` (``get_particle`` & co.), so does this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from ._native import B2DError
+
+MODE_REFERENCE = 0
+MODE_FAST = 1
+COLLIDE_PP = 1
+COLLIDE_PC = 2
+COLLIDE_PPOLY = 4
+
+
+def _v(p) -> tuple:
+    return (float(p[0]), float(p[1]))
+
+
+@dataclass
+class Particle:
+    """src/particle.rs:4-9 (``acc`` is private there; exposed read-only here)."""
+    pos: tuple
+    prev_pos: tuple
+    acc: tuple = (0.0, 0.0)
+
+    @staticmethod
+    def new(pos) -> "Particle":  # src/particle.rs:12-18
+        p = _v(pos)
+        return Particle(p, p, (0.0, 0.0))
+
+
+@dataclass
+class Link:
+    """src/link.rs:4-10; particle_a must be lower than particle_b."""
+    particle_a: int
+    particle_b: int
+    target_distance: float
+    stiffness: float = 1.0  # extension; 1.0 reproduces the reference
+
+
+@dataclass
+class ParticleLink:  # src/link.rs:12-15
+    link: Link
+
+
+@dataclass
+class CircleLink:  # src/link.rs:30-33
+    link: Link
+
+
+@dataclass
+class Circle:  # src/circle.rs:4-8
+    point: Particle
+    radius: float
+    is_static: bool = False  # extension
+
+
+@dataclass
+class Bounds:  # src/solver.rs:13-17
+    pos: tuple
+    size: tuple
+
+
+@dataclass
+class Polygon:  # src/polygon.rs:7-14
+    particles: list
+    particle_links: list
+    is_static: bool
+    center: tuple
+    scale: float = 1.0
+
+    @staticmethod
+    def circle(radius: float, pos, point_count: int, is_static: bool) -> "Polygon":
+        """Polygon::circle, src/polygon.rs:17-82 (built by the native host code)."""
+        s = Solver()
+        s._chk(s._lib.b2d_add_polygon_circle(s._h, radius, N.Vec2(*_v(pos)), point_count,
+                                             int(is_static)))
+        return s.get_polygon(0)
+
+    @staticmethod
+    def new(points: Sequence, is_static: bool) -> "Polygon":
+        """Polygon::new, src/polygon.rs:84-123 (built by the native host code)."""
+        s = Solver()
+        pts = (N.Vec2 * len(points))(*[N.Vec2(*_v(p)) for p in points])
+        s._chk(s._lib.b2d_add_polygon_points(s._h, len(points), pts, int(is_static)))
+        return s.get_polygon(0)
+
+
+def _cpart(p: Particle) -> N.CParticle:
+    return N.CParticle(N.Vec2(*p.pos), N.Vec2(*p.prev_pos), N.Vec2(*p.acc))
+
+
+def _ppart(c: N.CParticle) -> Particle:
+    return Particle((c.pos.x, c.pos.y), (c.prev_pos.x, c.prev_pos.y), (c.acc.x, c.acc.y))
+
+
+def _f32p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Solver:
+    """src/solver.rs:19-189 — state lives on the GPU between updates."""
+
+    def __init__(self):
+        self._lib = N.load()
+        h = C.c_void_p()
+        N.check(self._lib.b2d_solver_create(C.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def new() -> "Solver":  # src/solver.rs:34-50
+        return Solver()
+
+    def _chk(self, code: int) -> None:
+        N.check(code)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.b2d_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clone(self) -> "Solver":  # #[derive(Clone)], src/solver.rs:19
+        out = Solver.__new__(Solver)
+        out._lib = self._lib
+        h = C.c_void_p()
+        self._chk(self._lib.b2d_solver_clone(self._h, C.byref(h)))
+        out._h = h
+        return out
+
+    # ---- pub fields (src/solver.rs:21-23)
+    @property
+    def gravity(self) -> tuple:
+        v = N.Vec2()
+        self._chk(self._lib.b2d_get_gravity(self._h, C.byref(v)))
+        return (v.x, v.y)
+
+    @gravity.setter
+    def gravity(self, g) -> None:
+        self._chk(self._lib.b2d_set_gravity(self._h, *_v(g)))
+
+    @property
+    def bounds(self) -> Bounds:
+        p, s = N.Vec2(), N.Vec2()
+        self._chk(self._lib.b2d_get_bounds(self._h, C.byref(p), C.byref(s)))
+        return Bounds((p.x, p.y), (s.x, s.y))
+
+    @bounds.setter
+    def bounds(self, b: Bounds) -> None:
+        self._chk(self._lib.b2d_set_bounds(self._h, *_v(b.pos), *_v(b.size)))
+
+    @property
+    def bounds_active(self) -> bool:
+        v = C.c_int()
+        self._chk(self._lib.b2d_get_bounds_active(self._h, C.byref(v)))
+        return bool(v.value)
+
+    @bounds_active.setter
+    def bounds_active(self, on: bool) -> None:
+        self._chk(self._lib.b2d_set_bounds_active(self._h, int(on)))
+
+    # ---- add_* (src/solver.rs:52-67)
+    def add_particle(self, pos) -> None:
+        self._chk(self._lib.b2d_add_particle(self._h, *_v(pos)))
+
+    def add_circle(self, circle: Circle) -> None:
+        c = N.CCircle(_cpart(circle.point), circle.radius, int(circle.is_static))
+        self._chk(self._lib.b2d_add_circle(self._h, C.byref(c)))
+
+    def add_polygon(self, polygon: Polygon) -> None:
+        nv, nl = len(polygon.particles), len(polygon.particle_links)
+        v = (N.CParticle * max(nv, 1))(*[_cpart(p) for p in polygon.particles])
+        links = []
+        for pl in polygon.particle_links:
+            l = pl.link if isinstance(pl, ParticleLink) else pl
+            links.append(N.CLink(l.particle_a, l.particle_b, l.target_distance, 1.0))
+        la = (N.CLink * max(nl, 1))(*links)
+        self._chk(self._lib.b2d_add_polygon(self._h, nv, v, nl, la, int(polygon.is_static),
+                                            N.Vec2(*polygon.center), polygon.scale))
+
+    def add_particle_link(self, link) -> None:
+        l = link.link if isinstance(link, ParticleLink) else link
+        if l.stiffness == 1.0:
+            self._chk(self._lib.b2d_add_particle_link(self._h, l.particle_a, l.particle_b,
+                                                      l.target_distance))
+        else:
+            self.add_particle_links([l.particle_a], [l.particle_b], [l.target_distance],
+                                    [l.stiffness])
+
+    def add_circle_link(self, link) -> None:
+        l = link.link if isinstance(link, CircleLink) else link
+        self._chk(self._lib.b2d_add_circle_link(self._h, l.particle_a, l.particle_b,
+                                                l.target_distance))
+
+    # ---- extension: bulk and initial velocity
+    def add_particle_prev(self, pos, prev) -> None:
+        self._chk(self._lib.b2d_add_particle_prev(self._h, *_v(pos), *_v(prev)))
+
+    def add_particles(self, pos: np.ndarray, prev: Optional[np.ndarray] = None) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 2)
+        if prev is not None:
+            prev = np.ascontiguousarray(prev, dtype=np.float32).reshape(-1, 2)
+        self._chk(self._lib.b2d_add_particles(self._h, len(pos), _f32p(pos), _f32p(prev)))
+
+    def add_particle_links(self, a, b, target, stiffness=None) -> None:
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        k = None if stiffness is None else np.ascontiguousarray(stiffness, dtype=np.float32)
+        u64 = C.POINTER(C.c_uint64)
+        self._chk(self._lib.b2d_add_particle_links(self._h, len(a), a.ctypes.data_as(u64),
+                                                   b.ctypes.data_as(u64), _f32p(t), _f32p(k)))
+
+    def add_polygon_circle(self, radius, pos, point_count, is_static) -> None:
+        self._chk(self._lib.b2d_add_polygon_circle(self._h, radius, N.Vec2(*_v(pos)),
+                                                   point_count, int(is_static)))
+
+    def add_polygon_points(self, points, is_static) -> None:
+        pts = (N.Vec2 * max(len(points), 1))(*[N.Vec2(*_v(p)) for p in points])
+        self._chk(self._lib.b2d_add_polygon_points(self._h, len(points), pts, int(is_static)))
+
+    # ---- extension knobs
+    @property
+    def sub_steps(self) -> int:
+        v = C.c_uint32()
+        self._chk(self._lib.b2d_get_sub_steps(self._h, C.byref(v)))
+        return v.value
+
+    def set_sub_steps(self, n: int) -> None:
+        self._chk(self._lib.b2d_set_sub_steps(self._h, n))
+
+    def set_link_iters(self, n: int) -> None:
+        self._chk(self._lib.b2d_set_link_iters(self._h, n))
+
+    def set_mode(self, mode: int) -> None:
+        self._chk(self._lib.b2d_set_mode(self._h, mode))
+
+    def set_collision(self, flags: int, particle_radius: float = 0.5, grid_cell: float = 1.0):
+        self._chk(self._lib.b2d_set_collision(self._h, flags, particle_radius, grid_cell))
+
+    def set_circle_static(self, index: int, is_static: bool) -> None:
+        self._chk(self._lib.b2d_set_circle_static(self._h, index, int(is_static)))
+
+    # ---- update (src/solver.rs:106-116)
+    def update(self, dt: float) -> None:
+        self._chk(self._lib.b2d_update(self._h, dt))
+
+    # ---- getters (src/solver.rs:69-104)
+    def _len(self, fn) -> int:
+        v = C.c_size_t()
+        self._chk(fn(self._h, C.byref(v)))
+        return v.value
+
+    def get_particle_len(self) -> int:
+        return self._len(self._lib.b2d_get_particle_len)
+
+    def get_circles_len(self) -> int:
+        return self._len(self._lib.b2d_get_circles_len)
+
+    def get_polygons_len(self) -> int:
+        return self._len(self._lib.b2d_get_polygons_len)
+
+    def _links(self, lenfn, getfn, wrap) -> list:
+        n = self._len(lenfn)
+        buf = (N.CLink * max(n, 1))()
+        self._chk(getfn(self._h, buf, n))
+        return [wrap(Link(buf[i].particle_a, buf[i].particle_b, buf[i].target_distance,
+                          buf[i].stiffness)) for i in range(n)]
+
+    def get_particle_links(self) -> list:
+        return self._links(self._lib.b2d_get_particle_links_len, self._lib.b2d_get_particle_links,
+                           ParticleLink)
+
+    def get_circle_links(self) -> list:
+        return self._links(self._lib.b2d_get_circle_links_len, self._lib.b2d_get_circle_links,
+                           CircleLink)
+
+    def get_particles(self) -> list:
+        n = self.get_particle_len()
+        buf = (N.CParticle * max(n, 1))()
+        self._chk(self._lib.b2d_get_particles(self._h, buf, n))
+        return [_ppart(buf[i]) for i in range(n)]
+
+    def get_circles(self) -> list:
+        n = self.get_circles_len()
+        buf = (N.CCircle * max(n, 1))()
+        self._chk(self._lib.b2d_get_circles(self._h, buf, n))
+        return [Circle(_ppart(buf[i].point), buf[i].radius, bool(buf[i].is_static))
+                for i in range(n)]
+
+    def get_polygons(self) -> list:
+        return [self.get_polygon(i) for i in range(self.get_polygons_len())]
+
+    def get_particle(self, index: int) -> Optional[Particle]:
+        c = N.CParticle()
+        code = self._lib.b2d_get_particle(self._h, index, C.byref(c))
+        if code == 6:
+            return None
+        self._chk(code)
+        return _ppart(c)
+
+    def get_circle(self, index: int) -> Optional[Circle]:
+        c = N.CCircle()
+        code = self._lib.b2d_get_circle(self._h, index, C.byref(c))
+        if code == 6:
+            return None
+        self._chk(code)
+        return Circle(_ppart(c.point), c.radius, bool(c.is_static))
+
+    def get_polygon(self, index: int) -> Optional[Polygon]:
+        nv, nl = C.c_size_t(), C.c_size_t()
+        st, ctr, sc = C.c_int(), N.Vec2(), C.c_float()
+        code = self._lib.b2d_get_polygon_info(self._h, index, C.byref(nv), C.byref(nl),
+                                              C.byref(st), C.byref(ctr), C.byref(sc))
+        if code == 6:
+            return None
+        self._chk(code)
+        vb = (N.CParticle * max(nv.value, 1))()
+        lb = (N.CLink * max(nl.value, 1))()
+        self._chk(self._lib.b2d_get_polygon(self._h, index, vb, nv.value, lb, nl.value))
+        parts = [_ppart(vb[i]) for i in range(nv.value)]
+        links = [ParticleLink(Link(lb[i].particle_a, lb[i].particle_b, lb[i].target_distance))
+                 for i in range(nl.value)]
+        return Polygon(parts, links, bool(st.value), (ctr.x, ctr.y), sc.value)
+
+    # ---- bulk state
+    def read_state(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.get_particle_len()
+        pos = np.empty((n, 2), np.float32)
+        prev = np.empty((n, 2), np.float32)
+        self._chk(self._lib.b2d_read_state(self._h, _f32p(pos), _f32p(prev)))
+        return pos, prev
+
+    def write_state(self, pos: np.ndarray, prev: np.ndarray) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        prev = np.ascontiguousarray(prev, dtype=np.float32)
+        self._chk(self._lib.b2d_write_state(self._h, _f32p(pos), _f32p(prev)))
+
+    # ---- execution control
+    def set_stream(self, stream_ptr: int) -> None:
+        self._chk(self._lib.b2d_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def synchronize(self) -> None:
+        self._chk(self._lib.b2d_synchronize(self._h))
+
+    def set_graphs(self, on: bool) -> None:
+        self._chk(self._lib.b2d_set_graphs(self._h, int(on)))
+
+    def set_profiling(self, on: bool) -> None:
+        self._chk(self._lib.b2d_set_profiling(self._h, int(on)))
+
+    def profile(self) -> dict:
+        return _profile(self._lib.b2d_get_profile, self._h)
+
+    def launch_count(self) -> int:
+        v = C.c_uint32()
+        self._chk(self._lib.b2d_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def state_bytes(self) -> int:
+        return self._len(self._lib.b2d_state_bytes)
+
+    def state_upload_async(self, host_ptr: int) -> None:
+        self._chk(self._lib.b2d_state_upload_async(self._h, C.c_void_p(host_ptr)))
+
+    def state_download_async(self, host_ptr: int) -> None:
+        self._chk(self._lib.b2d_state_download_async(self._h, C.c_void_p(host_ptr)))
+
+    def plan_stats(self) -> dict:
+        s = N.CPlanStats()
+        self._chk(self._lib.b2d_get_plan_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.CPlanStats._fields_}
+
+    def link_order(self) -> np.ndarray:
+        n = self._len(self._lib.b2d_get_particle_links_len)
+        out = np.empty(n, np.uint64)
+        self._chk(self._lib.b2d_get_link_order(self._h, out.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                               n))
+        return out
+
+
+def _profile(fn, h) -> dict:
+    names = C.create_string_buffer(4096)
+    ms = (C.c_float * 64)()
+    cnt = C.c_size_t()
+    N.check(fn(h, names, 4096, ms, 64, C.byref(cnt)))
+    keys = names.value.decode().split("\n") if cnt.value else []
+    return {k: ms[i] for i, k in enumerate(keys)}
+
+
+class Batch:
+    """Many independent solvers stepped by one launch sequence (extension)."""
+
+    def __init__(self, solvers: Iterable[Solver] = ()):
+        self._lib = N.load()
+        h = C.c_void_p()
+        N.check(self._lib.b2d_batch_create(C.byref(h)))
+        self._h = h
+        self.members: list[Solver] = []
+        for s in solvers:
+            self.add(s)
+
+    def add(self, s: Solver) -> None:
+        N.check(self._lib.b2d_batch_add(self._h, s._h))
+        self.members.append(s)
+
+    def remove(self, s: Solver) -> None:
+        N.check(self._lib.b2d_batch_remove(self._h, s._h))
+        self.members.remove(s)
+
+    def update(self, dt: float) -> None:
+        N.check(self._lib.b2d_batch_update(self._h, dt))
+
+    def synchronize(self) -> None:
+        N.check(self._lib.b2d_batch_synchronize(self._h))
+
+    def set_stream(self, stream_ptr: int) -> None:
+        N.check(self._lib.b2d_batch_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def set_profiling(self, on: bool) -> None:
+        N.check(self._lib.b2d_batch_set_profiling(self._h, int(on)))
+
+    def profile(self) -> dict:
+        return _profile(self._lib.b2d_batch_get_profile, self._h)
+
+    def launch_count(self) -> int:
+        v = C.c_uint32()
+        N.check(self._lib.b2d_batch_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.b2d_batch_destroy(self._h)
+            self._h = None
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,98 @@
+// b2d_dev.h — records shared by the host planner and the CUDA kernels.
+//
+// Device layout: every world (one Solver) is a self-contained block of device
+// memory holding all of its arrays; a DWorld record (in a device table) holds
+// the world's parameters and pointers into its block.  Work lists name
+// (world, item) pairs, so a batch or a serving pool is just a table of worlds.
+// Solver particles stay in insertion order, exactly like the reference's
+// Vec<Particle> (src/solver.rs:24).
+#pragma once
+#include <cstdint>
+
+// CUDA's vector types (plain C structs, usable by the host compiler too)
+#include <vector_functions.h>
+#include <vector_types.h>
+
+namespace b2d {
+
+// Collision extension flags (not in the reference; see solve_dynamic_collisions).
+enum : uint32_t { COLLIDE_PP = 1u, COLLIDE_PC = 2u, COLLIDE_PPOLY = 4u };
+
+// Schedule op encoding: link ops carry the body-local link index; bounds +
+// integrate ops carry the body-local particle index with this bit set.
+constexpr uint32_t OP_INTEG = 0x80000000u;
+
+// A body is a set of solver particles run by one executor unit: a union of
+// whole link-connected components, so no link crosses two bodies.
+struct DBody {
+  uint32_t i0, np;       // particle list bidx[i0 .. i0+np) (world indices, ascending)
+  uint32_t l0, nl;       // links lab[l0 .. l0+nl) in insertion order
+  uint32_t sched;        // schedule id (group executors), else unused
+  uint32_t local;        // 1: link endpoints are body-local; 0: world indices
+};
+
+struct DPoly {
+  uint32_t v0, nv;       // vertices
+  uint32_t l0, nl;       // polygon links (polygon-local indices)
+  uint32_t is_static, pad;
+};
+
+struct DSched {
+  uint32_t lvl0, nlvl;   // level offsets at lvl[lvl0 .. lvl0+nlvl]
+  uint32_t op0, nops;    // ops at ops[op0 .. op0+nops)
+};
+
+struct DWorld {
+  // parameters
+  float gx, gy;          // 0 + gravity: the acceleration at integrate time
+  float bx, by, bw, bh;  // Bounds pos / size (src/solver.rs:13-17)
+  float h;               // dt * (1 / sub_steps) (src/solver.rs:107-108)
+  float radius, cell;    // extension: particle radius, grid cell
+  uint32_t S, I;         // sub_steps, link iterations
+  uint32_t flags;        // COLLIDE_* bits
+  uint32_t slot;         // stable id (hash salt for the shared grid)
+  uint32_t np, nb, nc, ncl, ng;
+  uint32_t pad;
+  // solver particles
+  float2* pos[2];        // ping-pong positions; pos[0] holds the state between steps
+  float2* prev;
+  // bodies and links
+  DBody* bodies;
+  uint32_t* bidx;
+  uint2* lab;
+  float* lrest;
+  float* lstiff;
+  // circles (src/circle.rs:4-8) and circle links
+  float2* cpos; float2* cprev; float2* cacc;
+  float* crad; uint32_t* cstatic;
+  uint2* clab; float* clrest;
+  // polygons (src/polygon.rs:7-14)
+  DPoly* polys;
+  float2* vpos; float2* vprev; float2* vacc;
+  float2* pcenter;
+  float4* paabb;
+  uint2* plab; float* plrest;
+  uint32_t* stage_off;   // polygon-pair test offsets, see rigid_phase_a
+};
+
+// Shared (engine-wide) read-only schedule registry.
+struct DScheds {
+  const DSched* scheds;
+  const uint32_t* lvl;
+  const uint32_t* ops;
+};
+
+// Extension broadphase: hashed uniform grid with K slots per bucket and an
+// overflow list sized so that nothing is ever dropped.
+constexpr uint32_t BUCKET_K = 8;
+struct DGrid {
+  uint32_t* count;       // nbuckets
+  uint4* slots;          // nbuckets * BUCKET_K : {world, particle, cx, cy}
+  uint4* overflow;       // cap entries
+  uint32_t* ovf_bucket;  // cap entries
+  uint32_t* ovf_n;       // [0] = used
+  uint32_t ovf_cap;
+  uint32_t mask;         // nbuckets - 1
+};
+
+}  // namespace b2d

@@ -1,0 +1,603 @@
+// engine.cu — device memory, work lists and the launch sequence of one
+// Solver::update over every world an Engine holds.
+//
+// Step structure (src/solver.rs:106-116):
+//  * worlds without extension collisions: every body runs the whole step
+//    (all sub-steps, link iterations, bounds, integration) in one launch of
+//    the group or serial executor; circles and polygons run in one CTA per
+//    world (k_rigid<0>).
+//  * worlds with extension collisions: per sub-step, link passes (group /
+//    serial executors), circle+polygon phase, grid insert, then collide +
+//    bounds + integrate; positions ping-pong between two buffers.
+// The whole sequence is captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "engine.hpp"
+#include "kernels.cuh"
+
+namespace b2d {
+
+#define B2D_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      last_error = std::string(#call) + ": " + cudaGetErrorString(e_);        \
+      return ERR_CUDA;                                                        \
+    }                                                                         \
+  } while (0)
+
+static uint32_t pow2ceil_u(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+static int g_smem_optin = -1;
+
+Engine::Engine(cudaStream_t stream) : stream_(stream) {
+  if (!stream_) {
+    cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+    own_stream_ = true;
+  }
+  if (g_smem_optin < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g_smem_optin = v;
+    cudaFuncSetAttribute(k_exec_groups<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    cudaFuncSetAttribute(k_exec_groups<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  }
+  tune_.smem_max = std::min<uint32_t>(tune_.smem_max, (uint32_t)std::max(g_smem_optin, 48 * 1024));
+}
+
+Engine::~Engine() {
+  if (graph_) cudaGraphExecDestroy(graph_);
+  cudaStreamSynchronize(stream_);
+  for (Slot& s : slots_)
+    if (s.block) cudaFree(s.block);
+  cudaFree(d_worlds_);
+  cudaFree(d_scheds_);
+  cudaFree(d_lvl_);
+  cudaFree(d_ops_);
+  cudaFree(d_lists_);
+  cudaFree(d_wlists_);
+  cudaFree(d_grid_);
+  if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::invalidate_graph() {
+  if (graph_) {
+    cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+  }
+  graph_valid_ = false;
+}
+
+void Engine::set_stream(cudaStream_t s) {
+  cudaStreamSynchronize(stream_);
+  if (own_stream_) cudaStreamDestroy(stream_);
+  own_stream_ = false;
+  stream_ = s;
+  if (!stream_) {
+    cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+    own_stream_ = true;
+  }
+  invalidate_graph();
+}
+
+const WorldImage* Engine::image(uint32_t slot) const {
+  if (slot >= slots_.size() || !slots_[slot].live) return nullptr;
+  return &slots_[slot].img;
+}
+
+int Engine::ensure_table(size_t n) {
+  if (n <= worlds_cap_) return OK;
+  size_t cap = std::max<size_t>(n, worlds_cap_ * 2 + 4);
+  DWorld* d = nullptr;
+  B2D_CUDA(cudaMalloc(&d, cap * sizeof(DWorld)));
+  if (d_worlds_) {
+    B2D_CUDA(cudaMemcpyAsync(d, d_worlds_, worlds_cap_ * sizeof(DWorld), cudaMemcpyDeviceToDevice, stream_));
+    B2D_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(d_worlds_);
+  }
+  d_worlds_ = d;
+  worlds_cap_ = cap;
+  invalidate_graph();
+  return OK;
+}
+
+int Engine::fill_world_record(uint32_t slot) {
+  Slot& s = slots_[slot];
+  DWorld W = s.img.params;
+  const BlockLayout& L = s.L;
+  unsigned char* b = s.block;
+  W.pos[0] = reinterpret_cast<float2*>(b + L.o_pos);
+  W.pos[1] = reinterpret_cast<float2*>(b + L.o_pos1);
+  W.prev = reinterpret_cast<float2*>(b + L.o_prev);
+  W.bodies = reinterpret_cast<DBody*>(b + L.o_bodies);
+  W.bidx = reinterpret_cast<uint32_t*>(b + L.o_bidx);
+  W.lab = reinterpret_cast<uint2*>(b + L.o_lab);
+  W.lrest = reinterpret_cast<float*>(b + L.o_lrest);
+  W.lstiff = reinterpret_cast<float*>(b + L.o_lstiff);
+  W.cpos = reinterpret_cast<float2*>(b + L.o_cpos);
+  W.cprev = reinterpret_cast<float2*>(b + L.o_cprev);
+  W.cacc = reinterpret_cast<float2*>(b + L.o_cacc);
+  W.crad = reinterpret_cast<float*>(b + L.o_crad);
+  W.cstatic = reinterpret_cast<uint32_t*>(b + L.o_cstatic);
+  W.clab = reinterpret_cast<uint2*>(b + L.o_clab);
+  W.clrest = reinterpret_cast<float*>(b + L.o_clrest);
+  W.polys = reinterpret_cast<DPoly*>(b + L.o_polys);
+  W.vpos = reinterpret_cast<float2*>(b + L.o_vpos);
+  W.vprev = reinterpret_cast<float2*>(b + L.o_vprev);
+  W.vacc = reinterpret_cast<float2*>(b + L.o_vacc);
+  W.pcenter = reinterpret_cast<float2*>(b + L.o_pcenter);
+  W.paabb = reinterpret_cast<float4*>(b + L.o_paabb);
+  W.plab = reinterpret_cast<uint2*>(b + L.o_plab);
+  W.plrest = reinterpret_cast<float*>(b + L.o_plrest);
+  W.stage_off = reinterpret_cast<uint32_t*>(b + L.o_stage);
+  W.h = s.dt * (1.0f / (float)W.S);  // src/solver.rs:107-108
+  if (h_worlds_.size() <= slot) h_worlds_.resize(slot + 1);
+  h_worlds_[slot] = W;
+  int st = ensure_table(slots_.size());
+  if (st != OK) return st;
+  B2D_CUDA(cudaMemcpyAsync(d_worlds_ + slot, &h_worlds_[slot], sizeof(DWorld),
+                           cudaMemcpyHostToDevice, stream_));
+  return OK;
+}
+
+int Engine::add(WorldHost* w, uint32_t* out_slot, std::string* why) {
+  uint32_t slot;
+  if (!free_slots_.empty()) {
+    slot = free_slots_.back();
+    free_slots_.pop_back();
+  } else {
+    slot = (uint32_t)slots_.size();
+    slots_.emplace_back();
+  }
+  Slot& s = slots_[slot];
+  int st = plan_world(*w, tune_, reg_, s.img, why);
+  if (st != OK) {
+    free_slots_.push_back(slot);
+    return st;
+  }
+  s.host = w;
+  s.L = layout_of(s.img);
+  B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&s.block), s.L.total, stream_));
+  dev_bytes_ += s.L.total;
+  std::vector<unsigned char> stage(s.L.total);
+  write_block(s.img, s.L, stage.data());
+  B2D_CUDA(cudaMemcpyAsync(s.block, stage.data(), s.L.total, cudaMemcpyHostToDevice, stream_));
+  s.live = true;
+  st = fill_world_record(slot);
+  if (st != OK) return st;
+  B2D_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is pageable
+  lists_dirty_ = true;
+  *out_slot = slot;
+  return OK;
+}
+
+int Engine::remove(uint32_t slot) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  Slot& s = slots_[slot];
+  B2D_CUDA(cudaFreeAsync(s.block, stream_));
+  dev_bytes_ -= s.L.total;
+  s = Slot();
+  free_slots_.push_back(slot);
+  lists_dirty_ = true;
+  return OK;
+}
+
+int Engine::set_dt(uint32_t slot, float dt) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  Slot& s = slots_[slot];
+  if (s.dt == dt && h_worlds_[slot].h == dt * (1.0f / (float)h_worlds_[slot].S)) return OK;
+  s.dt = dt;
+  h_worlds_[slot].h = dt * (1.0f / (float)h_worlds_[slot].S);  // src/solver.rs:107-108
+  B2D_CUDA(cudaMemcpyAsync(&d_worlds_[slot].h, &h_worlds_[slot].h, sizeof(float),
+                           cudaMemcpyHostToDevice, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  return OK;
+}
+
+int Engine::set_params(uint32_t slot) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  Slot& s = slots_[slot];
+  const WorldHost& w = *s.host;
+  DWorld& W = h_worlds_[slot];
+  W.gx = 0.0f + w.gravity.x;
+  W.gy = 0.0f + w.gravity.y;
+  W.bx = w.bounds.pos.x;
+  W.by = w.bounds.pos.y;
+  W.bw = w.bounds.size.x;
+  W.bh = w.bounds.size.y;
+  s.img.params.gx = W.gx; s.img.params.gy = W.gy;
+  s.img.params.bx = W.bx; s.img.params.by = W.by;
+  s.img.params.bw = W.bw; s.img.params.bh = W.bh;
+  B2D_CUDA(cudaMemcpyAsync(d_worlds_ + slot, &W, sizeof(DWorld), cudaMemcpyHostToDevice, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  return OK;
+}
+
+int Engine::upload_registry() {
+  auto grow = [&](auto*& ptr, size_t& cap, size_t need, size_t elem) -> int {
+    if (need <= cap) return OK;
+    size_t nc = std::max(need, cap * 2 + 1024);
+    void* d = nullptr;
+    B2D_CUDA(cudaMalloc(&d, nc * elem));
+    B2D_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(ptr);
+    ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(d);
+    cap = nc;
+    invalidate_graph();
+    return OK;
+  };
+  const bool grew = reg_.scheds.size() > scheds_cap_ || reg_.lvl.size() > lvl_cap_ ||
+                    reg_.ops.size() > ops_cap_;
+  int st;
+  if ((st = grow(d_scheds_, scheds_cap_, reg_.scheds.size(), sizeof(DSched))) != OK) return st;
+  if ((st = grow(d_lvl_, lvl_cap_, reg_.lvl.size(), 4)) != OK) return st;
+  if ((st = grow(d_ops_, ops_cap_, reg_.ops.size(), 4)) != OK) return st;
+  if (grew) reg_.uploaded_scheds = reg_.uploaded_lvl = reg_.uploaded_ops = 0;
+  auto put = [&](void* dst, const void* src, size_t from, size_t to, size_t elem) -> int {
+    if (to > from)
+      B2D_CUDA(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + from * elem,
+                               static_cast<const unsigned char*>(src) + from * elem,
+                               (to - from) * elem, cudaMemcpyHostToDevice, stream_));
+    return OK;
+  };
+  if ((st = put(d_scheds_, reg_.scheds.data(), reg_.uploaded_scheds, reg_.scheds.size(), sizeof(DSched))) != OK) return st;
+  if ((st = put(d_lvl_, reg_.lvl.data(), reg_.uploaded_lvl, reg_.lvl.size(), 4)) != OK) return st;
+  if ((st = put(d_ops_, reg_.ops.data(), reg_.uploaded_ops, reg_.ops.size(), 4)) != OK) return st;
+  reg_.uploaded_scheds = reg_.scheds.size();
+  reg_.uploaded_lvl = reg_.lvl.size();
+  reg_.uploaded_ops = reg_.ops.size();
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  return OK;
+}
+
+int Engine::ensure_grid(size_t np_ext) {
+  if (np_ext <= grid_np_ && d_grid_) return OK;
+  size_t nb = pow2ceil_u((uint32_t)std::max<size_t>(np_ext, 1024));
+  size_t cap = std::max<size_t>(np_ext, 1);
+  size_t bytes = 0;
+  auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
+  size_t o_count = seg(nb * 4), o_slots = seg(nb * BUCKET_K * 16), o_ovf = seg(cap * 16),
+         o_ovfb = seg(cap * 4), o_ovfn = seg(16);
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  cudaFree(d_grid_);
+  d_grid_ = nullptr;
+  B2D_CUDA(cudaMalloc(&d_grid_, bytes));
+  B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
+  grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
+  grid_.slots = reinterpret_cast<uint4*>(d_grid_ + o_slots);
+  grid_.overflow = reinterpret_cast<uint4*>(d_grid_ + o_ovf);
+  grid_.ovf_bucket = reinterpret_cast<uint32_t*>(d_grid_ + o_ovfb);
+  grid_.ovf_n = reinterpret_cast<uint32_t*>(d_grid_ + o_ovfn);
+  grid_.ovf_cap = (uint32_t)cap;
+  grid_.mask = (uint32_t)(nb - 1);
+  grid_np_ = np_ext;
+  invalidate_graph();
+  return OK;
+}
+
+int Engine::rebuild_lists() {
+  classes_.clear();
+  serial_full_.clear();
+  serial_links_.clear();
+  chunks_.clear();
+  rigid_full_.clear();
+  rigid_ext_.clear();
+  smax_ext_ = 0;
+  any_pp_ = false;
+  size_t np_ext = 0;
+  std::map<std::tuple<uint32_t, bool, bool, uint32_t>, size_t> cls;
+  for (uint32_t si = 0; si < slots_.size(); ++si) {
+    const Slot& s = slots_[si];
+    if (!s.live) continue;
+    const WorldImage& im = s.img;
+    const bool full = !im.ext;
+    for (const GroupBody& gb : im.groups) {
+      const uint32_t rc = gb.smem ? std::max<uint32_t>(pow2ceil_u(gb.region), 1024) : 0u;
+      auto key = std::make_tuple(gb.T, gb.smem, full, rc);
+      auto it = cls.find(key);
+      if (it == cls.end()) {
+        LaunchClass c;
+        c.T = gb.T;
+        c.smem = gb.smem;
+        c.full = full;
+        c.region = gb.smem ? std::min<uint32_t>(rc, tune_.smem_max) : 0u;
+        if (gb.smem && c.region < gb.region) c.region = gb.region;
+        uint32_t G = gb.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / gb.T);
+        if (gb.T != 32) G = std::min<uint32_t>(G, 15);
+        if (c.smem) G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / c.region));
+        c.G = G;
+        it = cls.emplace(key, classes_.size()).first;
+        classes_.push_back(std::move(c));
+      }
+      classes_[it->second].items.push_back(make_uint2(si, gb.body));
+    }
+    for (uint32_t b : im.serials) (full ? serial_full_ : serial_links_).push_back(make_uint2(si, b));
+    const bool rigid = im.params.nc > 0 || im.params.ng > 0;
+    if (full) {
+      if (rigid) rigid_full_.push_back(si);
+    } else {
+      if (rigid) rigid_ext_.push_back(si);
+      smax_ext_ = std::max(smax_ext_, im.params.S);
+      if (im.params.flags & COLLIDE_PP) any_pp_ = true;
+      for (uint32_t st = 0; st < im.params.np; st += CHUNK) chunks_.push_back(make_uint2(si, st));
+      np_ext += im.params.np;
+    }
+  }
+  // sort serial items longest first (load balance)
+  auto serial_cost = [&](const uint2& a) {
+    const DBody& B = slots_[a.x].img.bodies[a.y];
+    return (uint64_t)B.nl * slots_[a.x].img.params.I + B.np;
+  };
+  std::stable_sort(serial_full_.begin(), serial_full_.end(),
+                   [&](const uint2& a, const uint2& b) { return serial_cost(a) > serial_cost(b); });
+  std::stable_sort(serial_links_.begin(), serial_links_.end(),
+                   [&](const uint2& a, const uint2& b) { return serial_cost(a) > serial_cost(b); });
+  // upload lists
+  std::vector<uint2> all;
+  for (LaunchClass& c : classes_) {
+    c.dev_off = all.size();
+    all.insert(all.end(), c.items.begin(), c.items.end());
+  }
+  off_serial_full_ = all.size();
+  all.insert(all.end(), serial_full_.begin(), serial_full_.end());
+  off_serial_links_ = all.size();
+  all.insert(all.end(), serial_links_.begin(), serial_links_.end());
+  off_chunks_ = all.size();
+  all.insert(all.end(), chunks_.begin(), chunks_.end());
+  std::vector<uint32_t> wl(rigid_full_);
+  off_rigid_ext_ = wl.size();
+  wl.insert(wl.end(), rigid_ext_.begin(), rigid_ext_.end());
+  if (all.size() > lists_cap_) {
+    B2D_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(d_lists_);
+    lists_cap_ = std::max(all.size(), lists_cap_ * 2 + 64);
+    B2D_CUDA(cudaMalloc(&d_lists_, lists_cap_ * sizeof(uint2)));
+  }
+  if (wl.size() > wlists_cap_) {
+    B2D_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(d_wlists_);
+    wlists_cap_ = std::max(wl.size(), wlists_cap_ * 2 + 64);
+    B2D_CUDA(cudaMalloc(&d_wlists_, wlists_cap_ * sizeof(uint32_t)));
+  }
+  if (!all.empty())
+    B2D_CUDA(cudaMemcpyAsync(d_lists_, all.data(), all.size() * sizeof(uint2), cudaMemcpyHostToDevice, stream_));
+  if (!wl.empty())
+    B2D_CUDA(cudaMemcpyAsync(d_wlists_, wl.data(), wl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  if (np_ext > 0) {
+    int st = ensure_grid(np_ext);
+    if (st != OK) return st;
+  }
+  lists_dirty_ = false;
+  invalidate_graph();
+  return OK;
+}
+
+int Engine::launch_all(bool profiling) {
+  launches_ = 0;
+  prof_.clear();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (profiling) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+  }
+  auto timed = [&](const char* name, auto&& fn, bool kernel = true) {
+    if (profiling) cudaEventRecord(e0, stream_);
+    fn();
+    if (kernel) ++launches_;
+    if (profiling) {
+      cudaEventRecord(e1, stream_);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      bool found = false;
+      for (auto& p : prof_)
+        if (p.first == name) { p.second += ms; found = true; }
+      if (!found) prof_.emplace_back(name, ms);
+    }
+  };
+  const DScheds SC{d_scheds_, d_lvl_, d_ops_};
+  const DWorld* W = d_worlds_;
+  auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
+    for (const LaunchClass& c : classes_) {
+      if (c.full != full || c.items.empty()) continue;
+      const uint32_t n = (uint32_t)c.items.size();
+      const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
+      const size_t sm = c.smem ? (size_t)c.G * c.region : 0;
+      const uint2* L = d_lists_ + c.dev_off;
+      const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
+                              : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
+      timed(name, [&] {
+        if (full && c.smem) k_exec_groups<true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
+        else if (full) k_exec_groups<true, false><<<grid, block, 0, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
+        else if (c.smem) k_exec_groups<false, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
+        else k_exec_groups<false, false><<<grid, block, 0, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
+      });
+    }
+  };
+  // worlds without extension collisions: one launch per class for the whole step
+  groups(true, 0, 0);
+  if (!serial_full_.empty()) {
+    const uint32_t n = (uint32_t)serial_full_.size();
+    timed("exec_serial_full", [&] {
+      k_exec_serial<true><<<(n + 127) / 128, 128, 0, stream_>>>(W, d_lists_ + off_serial_full_, n, 0, 0);
+    });
+  }
+  if (!rigid_full_.empty()) {
+    const uint32_t n = (uint32_t)rigid_full_.size();
+    timed("rigid_full", [&] { k_rigid<0><<<n, 128, 0, stream_>>>(W, d_wlists_, n, 0); });
+  }
+  // worlds with extension collisions: per sub-step pipeline
+  const uint32_t nch = (uint32_t)chunks_.size();
+  const uint2* CH = d_lists_ + off_chunks_;
+  const uint32_t nre = (uint32_t)rigid_ext_.size();
+  const uint32_t* RE = d_wlists_ + off_rigid_ext_;
+  for (uint32_t s = 0; s < smax_ext_; ++s) {
+    const uint32_t cur = s & 1u;
+    groups(false, cur, s);
+    if (!serial_links_.empty()) {
+      const uint32_t n = (uint32_t)serial_links_.size();
+      timed("exec_serial_links", [&] {
+        k_exec_serial<false><<<(n + 127) / 128, 128, 0, stream_>>>(W, d_lists_ + off_serial_links_, n, cur, s);
+      });
+    }
+    if (nre) {
+      timed("rigid_ext", [&] {
+        if (s == 0) k_rigid<1><<<nre, 128, 0, stream_>>>(W, RE, nre, s);
+        else k_rigid<3><<<nre, 128, 0, stream_>>>(W, RE, nre, s);
+      });
+    }
+    if (any_pp_) {
+      timed("grid_clear", [&] {
+        cudaMemsetAsync(grid_.count, 0, ((size_t)grid_.mask + 1) * 4, stream_);
+        cudaMemsetAsync(grid_.ovf_n, 0, 8, stream_);
+      }, false);
+      timed("grid_insert", [&] {
+        k_grid_insert<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      });
+    }
+    timed("collide_integrate", [&] {
+      k_collide_integrate<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+    });
+  }
+  if (smax_ext_ > 0) {
+    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, 0, stream_>>>(W, RE, nre, smax_ext_ - 1); });
+    timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
+  }
+  if (profiling) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  B2D_CUDA(cudaGetLastError());
+  return OK;
+}
+
+int Engine::step() {
+  int st;
+  if (lists_dirty_ && (st = rebuild_lists()) != OK) return st;
+  if ((st = upload_registry()) != OK) return st;
+  if (profile_) return launch_all(true);
+  if (!use_graph_) return launch_all(false);
+  if (!graph_valid_) {
+    cudaGraph_t g = nullptr;
+    B2D_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    st = launch_all(false);
+    cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+    if (st != OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess) {
+      last_error = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce);
+      return ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      last_error = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie);
+      graph_ = nullptr;
+      return ERR_CUDA;
+    }
+    graph_valid_ = true;
+  }
+  B2D_CUDA(cudaGraphLaunch(graph_, stream_));
+  return OK;
+}
+
+int Engine::sync() {
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  return OK;
+}
+
+int Engine::state_span(uint32_t slot, void** dptr, size_t* bytes) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  *dptr = slots_[slot].block;
+  *bytes = slots_[slot].L.state_bytes;
+  return OK;
+}
+
+int Engine::download(uint32_t slot) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  Slot& s = slots_[slot];
+  std::vector<float2> buf(s.L.state_bytes / sizeof(float2));
+  if (!buf.empty())
+    B2D_CUDA(cudaMemcpyAsync(buf.data(), s.block, s.L.state_bytes, cudaMemcpyDeviceToHost, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  WorldHost& w = *s.host;
+  const float2* p = buf.data();
+  const size_t np = s.img.pos.size();
+  for (size_t i = 0; i < np; ++i) {
+    w.particles[i].pos = Vec2{p[i].x, p[i].y};
+    w.particles[i].prev_pos = Vec2{p[np + i].x, p[np + i].y};
+    w.particles[i].acc = Vec2{0.0f, 0.0f};
+  }
+  p += 2 * np;
+  const size_t nc = s.img.cpos.size();
+  for (size_t i = 0; i < nc; ++i) {
+    w.circles[i].point.pos = Vec2{p[i].x, p[i].y};
+    w.circles[i].point.prev_pos = Vec2{p[nc + i].x, p[nc + i].y};
+    w.circles[i].point.acc = Vec2{p[2 * nc + i].x, p[2 * nc + i].y};
+  }
+  p += 3 * nc;
+  const size_t nv = s.img.vpos.size();
+  size_t v = 0;
+  for (size_t g = 0; g < w.polygons.size(); ++g) {
+    Polygon& P = w.polygons[g];
+    for (Particle& q : P.particles) {
+      q.pos = Vec2{p[v].x, p[v].y};
+      q.prev_pos = Vec2{p[nv + v].x, p[nv + v].y};
+      q.acc = Vec2{p[2 * nv + v].x, p[2 * nv + v].y};
+      ++v;
+    }
+    P.center = Vec2{p[3 * nv + g].x, p[3 * nv + g].y};
+  }
+  return OK;
+}
+
+int Engine::upload_state(uint32_t slot) {
+  if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
+  Slot& s = slots_[slot];
+  const WorldHost& w = *s.host;
+  std::vector<float2> buf(s.L.state_bytes / sizeof(float2));
+  float2* p = buf.data();
+  const size_t np = w.particles.size();
+  for (size_t i = 0; i < np; ++i) {
+    p[i] = make_float2(w.particles[i].pos.x, w.particles[i].pos.y);
+    p[np + i] = make_float2(w.particles[i].prev_pos.x, w.particles[i].prev_pos.y);
+  }
+  p += 2 * np;
+  const size_t nc = w.circles.size();
+  for (size_t i = 0; i < nc; ++i) {
+    p[i] = make_float2(w.circles[i].point.pos.x, w.circles[i].point.pos.y);
+    p[nc + i] = make_float2(w.circles[i].point.prev_pos.x, w.circles[i].point.prev_pos.y);
+    p[2 * nc + i] = make_float2(w.circles[i].point.acc.x, w.circles[i].point.acc.y);
+  }
+  p += 3 * nc;
+  const size_t nv = s.img.vpos.size();
+  size_t v = 0;
+  for (size_t g = 0; g < w.polygons.size(); ++g) {
+    for (const Particle& q : w.polygons[g].particles) {
+      p[v] = make_float2(q.pos.x, q.pos.y);
+      p[nv + v] = make_float2(q.prev_pos.x, q.prev_pos.y);
+      p[2 * nv + v] = make_float2(q.acc.x, q.acc.y);
+      ++v;
+    }
+    p[3 * nv + g] = make_float2(w.polygons[g].center.x, w.polygons[g].center.y);
+  }
+  if (!buf.empty())
+    B2D_CUDA(cudaMemcpyAsync(s.block, buf.data(), s.L.state_bytes, cudaMemcpyHostToDevice, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  return OK;
+}
+
+}  // namespace b2d

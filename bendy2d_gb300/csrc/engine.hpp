@@ -1,0 +1,189 @@
+// engine.hpp — planner output (one world's device image) and the Engine that
+// owns device memory for a set of worlds and steps them together.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "b2d_dev.h"
+#include "host.hpp"
+
+typedef struct CUstream_st* cudaStream_t;
+typedef struct CUgraphExec_st* cudaGraphExec_t;
+
+namespace b2d {
+
+// Tunables of the planner (the autotuner sweeps these).
+struct PlanTuning {
+  float serial_width = 2.0f;        // single-pass width below which a body runs serially
+  uint32_t t_min = 32, t_max = 512; // threads per group
+  uint32_t pack_np = 1024;          // pack small components into bodies up to this size
+  uint32_t pack_nl = 4096;
+  uint32_t free_chunk = 2048;       // particles per body for link-free particles
+  uint32_t smem_max = 200 * 1024;   // bytes of shared memory per group region
+  uint32_t warp_groups = 8;         // groups per CTA when T == 32
+  float width_per_thread = 1.0f;    // T = pow2 >= avg width / this
+};
+
+// Engine-wide registry of level schedules, deduplicated by topology.
+struct SchedRegistry {
+  std::unordered_map<std::string, uint32_t> index;
+  std::vector<DSched> scheds;
+  std::vector<uint32_t> lvl;
+  std::vector<uint32_t> ops;
+  size_t uploaded_scheds = 0, uploaded_lvl = 0, uploaded_ops = 0;
+  uint32_t get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I, bool full);
+};
+
+struct GroupBody {
+  uint32_t body;
+  uint32_t T;
+  uint32_t region;  // shared bytes for this body (0 when run from global memory)
+  bool smem;
+};
+
+struct PlanStats {
+  uint32_t bodies = 0, group_bodies = 0, serial_bodies = 0, global_bodies = 0;
+  uint64_t levels = 0, ops = 0;  // summed over group bodies
+  uint32_t colours = 0;
+};
+
+// Device image of one world: exactly the arrays of its device block.
+struct WorldImage {
+  DWorld params{};   // parameters; pointers are filled at placement
+  bool ext = false;  // extension collisions on: per-sub-step pipeline
+  // state prefix (float2 each): pos, prev, cpos, cprev, cacc, vpos, vprev, vacc, pcenter
+  std::vector<float2> pos, prev, cpos, cprev, cacc, vpos, vprev, vacc, pcenter;
+  std::vector<uint32_t> bidx;
+  std::vector<DBody> bodies;
+  std::vector<uint2> lab;
+  std::vector<float> lrest, lstiff;
+  std::vector<float> crad;
+  std::vector<uint32_t> cstatic;
+  std::vector<uint2> clab;
+  std::vector<float> clrest;
+  std::vector<DPoly> polys;
+  std::vector<uint2> plab;
+  std::vector<float> plrest;
+  std::vector<uint32_t> stage_off;
+  std::vector<GroupBody> groups;
+  std::vector<uint32_t> serials;
+  std::vector<uint32_t> link_order;  // fast mode: world link order used
+  PlanStats stats;
+  size_t nv() const { return vpos.size(); }
+};
+
+int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, WorldImage& out,
+               std::string* why);
+
+// byte layout of a world block
+struct BlockLayout {
+  size_t state_bytes = 0, total = 0;
+  size_t o_pos, o_prev, o_cpos, o_cprev, o_cacc, o_vpos, o_vprev, o_vacc, o_pcenter;
+  size_t o_pos1, o_bidx, o_bodies, o_lab, o_lrest, o_lstiff, o_crad, o_cstatic, o_clab,
+      o_clrest, o_polys, o_paabb, o_plab, o_plrest, o_stage;
+};
+BlockLayout layout_of(const WorldImage& im);
+void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst);
+
+struct LaunchClass {
+  uint32_t T, G, region;
+  bool smem, full;
+  std::vector<uint2> items;
+  size_t dev_off = 0;  // offset (in uint2) into the device list buffer
+};
+
+class Engine {
+ public:
+  explicit Engine(cudaStream_t stream = nullptr);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  int add(WorldHost* w, uint32_t* slot, std::string* why);
+  int remove(uint32_t slot);
+  int set_dt(uint32_t slot, float dt);
+  int set_params(uint32_t slot);          // gravity / bounds changed on the host mirror
+  int step();                             // one Solver::update for every world
+  int download(uint32_t slot);            // device state -> host mirror
+  int upload_state(uint32_t slot);        // host mirror state -> device (same topology)
+  // raw state prefix (pos, prev, circles, polygons) of a world, for end-to-end
+  // transfers from and to pinned host memory
+  int state_span(uint32_t slot, void** dptr, size_t* bytes);
+  int sync();
+  void set_stream(cudaStream_t s);
+  cudaStream_t stream() const { return stream_; }
+  void set_use_graph(bool on) { use_graph_ = on; invalidate_graph(); }
+  void set_profile(bool on) { profile_ = on; }
+  // per-kernel timings of the last profiled step (ms), keyed by kernel name
+  const std::vector<std::pair<std::string, float>>& last_profile() const { return prof_; }
+  const WorldImage* image(uint32_t slot) const;
+  uint32_t launches_per_step() const { return launches_; }
+  PlanTuning& tuning() { return tune_; }
+  size_t device_bytes() const { return dev_bytes_; }
+  std::string last_error;
+
+ private:
+  struct Slot {
+    WorldHost* host = nullptr;
+    WorldImage img;
+    BlockLayout L;
+    unsigned char* block = nullptr;
+    float dt = 0.0f;
+    bool live = false;
+  };
+  int rebuild_lists();
+  int upload_registry();
+  int ensure_table(size_t n);
+  int ensure_grid(size_t np_ext);
+  int launch_all(bool profiling);
+  void invalidate_graph();
+  int fill_world_record(uint32_t slot);
+
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  PlanTuning tune_;
+  SchedRegistry reg_;
+  std::vector<Slot> slots_;
+  std::vector<uint32_t> free_slots_;
+  // device tables
+  DWorld* d_worlds_ = nullptr;
+  size_t worlds_cap_ = 0;
+  std::vector<DWorld> h_worlds_;
+  DSched* d_scheds_ = nullptr;
+  size_t scheds_cap_ = 0;
+  uint32_t* d_lvl_ = nullptr;
+  size_t lvl_cap_ = 0;
+  uint32_t* d_ops_ = nullptr;
+  size_t ops_cap_ = 0;
+  // work lists
+  std::vector<LaunchClass> classes_;
+  std::vector<uint2> serial_full_, serial_links_, chunks_;
+  std::vector<uint32_t> rigid_full_, rigid_ext_;
+  uint2* d_lists_ = nullptr;
+  size_t lists_cap_ = 0;
+  size_t off_serial_full_ = 0, off_serial_links_ = 0, off_chunks_ = 0;
+  uint32_t* d_wlists_ = nullptr;
+  size_t wlists_cap_ = 0;
+  size_t off_rigid_ext_ = 0;
+  uint32_t smax_ext_ = 0;
+  bool any_pp_ = false;
+  bool lists_dirty_ = true;
+  // broadphase
+  DGrid grid_{};
+  size_t grid_np_ = 0;
+  unsigned char* d_grid_ = nullptr;
+  // graph
+  bool use_graph_ = true;
+  cudaGraphExec_t graph_ = nullptr;
+  bool graph_valid_ = false;
+  bool profile_ = false;
+  std::vector<std::pair<std::string, float>> prof_;
+  uint32_t launches_ = 0;
+  size_t dev_bytes_ = 0;
+};
+
+}  // namespace b2d

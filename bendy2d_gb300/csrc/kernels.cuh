@@ -1,0 +1,852 @@
+// kernels.cuh — CUDA kernels for the bendy2d solver step (sm_103a).
+//
+// Every floating-point operation that has a counterpart in the reference uses
+// the round-to-nearest intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn,
+// __fsqrt_rn ...).  Those are never contracted into FMA and are IEEE exact, so
+// each op rounds exactly like the reference's scalar f32 arithmetic (rustc
+// does not contract either).  The file is also compiled with --fmad=false.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "b2d_dev.h"
+
+namespace b2d {
+
+#define B2D_NONE 0xFFFFFFFFu
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// nalgebra norm_squared is 0 + (x*x + y*y); a sum of two squares is never
+// -0, so adding the leading +0 cannot change the value and is omitted.
+__device__ __forceinline__ float norm_sq(float x, float y) { return fadd(fmul(x, x), fmul(y, y)); }
+__device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) {
+  return fadd(fmul(ax, bx), fmul(ay, by));
+}
+
+// ParticleLink::solve, src/link.rs:18-27:
+//   d = a - b; dist = |d|; n = d / dist;
+//   a -= n*(dist - L)*0.5; b += n*(dist - L)*0.5
+// Extension: the correction is multiplied by the stiffness last (1 = exact).
+__device__ __forceinline__ void link_solve(float2& a, float2& b, float rest, float stiff) {
+  float dx = fsub(a.x, b.x), dy = fsub(a.y, b.y);
+  float dist = fsqrt(norm_sq(dx, dy));
+  float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
+  float m = fsub(dist, rest);
+  float cx = fmul(fmul(fmul(nx, m), 0.5f), stiff);
+  float cy = fmul(fmul(fmul(ny, m), 0.5f), stiff);
+  a.x = fsub(a.x, cx); a.y = fsub(a.y, cy);
+  b.x = fadd(b.x, cx); b.y = fadd(b.y, cy);
+}
+
+// Particle::solve_bounds, src/particle.rs:27-46 (min side, else max side).
+__device__ __forceinline__ void solve_bounds(float2& p, float2& q, const DWorld& w) {
+  float hx = fadd(w.bx, w.bw), hy = fadd(w.by, w.bh);
+  if (p.x < w.bx) { float v = fsub(q.x, p.x); q.x = fsub(w.bx, v); p.x = w.bx; }
+  else if (p.x > hx) { float v = fsub(q.x, p.x); q.x = fsub(hx, v); p.x = hx; }
+  if (p.y < w.by) { float v = fsub(q.y, p.y); q.y = fsub(w.by, v); p.y = w.by; }
+  else if (p.y > hy) { float v = fsub(q.y, p.y); q.y = fsub(hy, v); p.y = hy; }
+}
+
+// Circle::solve_bounds, src/circle.rs:11-30 (bounds inset by the radius).
+__device__ __forceinline__ void circle_bounds(float2& p, float2& q, float r, const DWorld& w) {
+  float hx = fadd(w.bx, w.bw), hy = fadd(w.by, w.bh);
+  float lo_x = fadd(w.bx, r), hi_x = fsub(hx, r);
+  float lo_y = fadd(w.by, r), hi_y = fsub(hy, r);
+  if (p.x < lo_x) { float v = fsub(q.x, p.x); q.x = fsub(lo_x, v); p.x = lo_x; }
+  else if (p.x > hi_x) { float v = fsub(q.x, p.x); q.x = fsub(hi_x, v); p.x = hi_x; }
+  if (p.y < lo_y) { float v = fsub(q.y, p.y); q.y = fsub(lo_y, v); p.y = lo_y; }
+  else if (p.y > hi_y) { float v = fsub(q.y, p.y); q.y = fsub(hi_y, v); p.y = hi_y; }
+}
+
+// Particle::update, src/particle.rs:20-25: pos = (pos + vel) + (acc*dt)*dt.
+__device__ __forceinline__ void integrate(float2& p, float2& q, float ax, float ay, float h) {
+  float vx = fsub(p.x, q.x), vy = fsub(p.y, q.y);
+  q = p;
+  p.x = fadd(fadd(p.x, vx), fmul(fmul(ax, h), h));
+  p.y = fadd(fadd(p.y, vy), fmul(fmul(ay, h), h));
+}
+
+// Group barrier: a group is one warp (syncwarp) or a named barrier over T
+// threads.  Both order shared and global memory among the group's threads.
+__device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
+  if (T == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(T) : "memory");
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Body executor (block / warp granularity).
+//
+// Each CTA holds G groups of T threads; group g runs work item
+// list[blockIdx*G + g] = (world, body) through the body's level schedule.  A
+// level is a set of ops on pairwise disjoint particles, and the levels keep,
+// for every particle, the exact order of the reference's sequential loops, so
+// running a level in parallel reproduces Solver::update bit for bit.  FULL
+// schedules cover every sub-step of Solver::update (links x I, then bounds +
+// integrate, src/solver.rs:109-115); LINKS-only schedules cover the I link
+// passes of one sub-step (extension pipeline).
+//
+// SMEM: the body's positions (and prev) and links live in shared memory; the
+// op stream is read from global memory with a two-level register prefetch so
+// its latency stays off the per-level critical path.  !SMEM runs the same
+// schedule directly on global memory (bodies too large for shared memory).
+// ----------------------------------------------------------------------------
+template <bool FULL, bool SMEM>
+__global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
+                              const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
+                              uint32_t G, uint32_t region_bytes, uint32_t cur, uint32_t sub) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
+  const uint32_t item = blockIdx.x * G + g;
+  if (item >= nlist) return;  // the whole group leaves; its barrier is private
+  const uint2 wi = list[item];
+  const DWorld& W = worlds[wi.x];
+  if (!FULL && sub >= W.S) return;  // world already finished its sub-steps
+  const DBody B = W.bodies[wi.y];
+  const uint32_t* bidx = W.bidx + B.i0;
+  float2* gp = W.pos[cur];
+  float2* gq = W.prev;
+  const uint2* gab = W.lab + B.l0;
+  const float* grest = W.lrest + B.l0;
+  const float* gstiff = W.lstiff + B.l0;
+  const float gx = W.gx, gy = W.gy, h = W.h;
+  DWorld Wb;  // bounds only
+  Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+
+  float2* sp = nullptr;
+  float2* sq = nullptr;
+  uint32_t* sab = nullptr;
+  float* srest = nullptr;
+  float* sstiff = nullptr;
+  if (SMEM) {
+    unsigned char* base = smem + (size_t)g * region_bytes;
+    sp = reinterpret_cast<float2*>(base);
+    sq = sp + B.np;
+    sab = reinterpret_cast<uint32_t*>(sq + (FULL ? B.np : 0));
+    srest = reinterpret_cast<float*>(sab + B.nl);
+    sstiff = srest + B.nl;
+    for (uint32_t i = t; i < B.np; i += T) {
+      const uint32_t k = bidx[i];
+      sp[i] = gp[k];
+      if (FULL) sq[i] = gq[k];
+    }
+    for (uint32_t i = t; i < B.nl; i += T) {
+      const uint2 ab = gab[i];
+      sab[i] = ab.x | (ab.y << 16);
+      srest[i] = grest[i];
+      sstiff[i] = gstiff[i];
+    }
+    group_sync(g, T);
+  }
+
+  auto run = [&](uint32_t op) {
+    if (op == B2D_NONE) return;
+    if (op & OP_INTEG) {
+      const uint32_t i = op & ~OP_INTEG;
+      float2* pp = SMEM ? sp + i : gp + bidx[i];
+      float2* qq = SMEM ? sq + i : gq + bidx[i];
+      float2 p = *pp, q = *qq;
+      solve_bounds(p, q, Wb);
+      integrate(p, q, gx, gy, h);
+      *pp = p;
+      *qq = q;
+    } else {
+      float2* pa;
+      float2* pb;
+      float rest, stiff;
+      if (SMEM) {
+        const uint32_t ab = sab[op];
+        pa = sp + (ab & 0xFFFFu);
+        pb = sp + (ab >> 16);
+        rest = srest[op];
+        stiff = sstiff[op];
+      } else {
+        const uint2 ab = gab[op];
+        pa = gp + ab.x;
+        pb = gp + ab.y;
+        rest = grest[op];
+        stiff = gstiff[op];
+      }
+      float2 a = *pa, b = *pb;
+      link_solve(a, b, rest, stiff);
+      *pa = a;
+      *pb = b;
+    }
+  };
+
+  const DSched S = SC.scheds[B.sched];
+  const uint32_t* __restrict__ lv = SC.lvl + S.lvl0;
+  const uint32_t* __restrict__ ops = SC.ops + S.op0;
+  const uint32_t nl = S.nlvl;
+  auto lvat = [&](uint32_t i) { return __ldg(lv + (i < nl ? i : nl)); };
+  uint32_t b0 = 0, e0 = lvat(1), e1 = lvat(2), e2 = lvat(3);
+  uint32_t o0 = (b0 + t < e0) ? __ldg(ops + b0 + t) : B2D_NONE;
+  uint32_t o1 = (e0 + t < e1) ? __ldg(ops + e0 + t) : B2D_NONE;
+  for (uint32_t l = 0; l < nl; ++l) {
+    const uint32_t o2 = (e1 + t < e2) ? __ldg(ops + e1 + t) : B2D_NONE;
+    const uint32_t e3 = lvat(l + 4);
+    run(o0);
+    for (uint32_t k = b0 + t + T; k < e0; k += T) run(__ldg(ops + k));
+    group_sync(g, T);
+    b0 = e0; e0 = e1; e1 = e2; e2 = e3;
+    o0 = o1; o1 = o2;
+  }
+
+  if (SMEM) {
+    for (uint32_t i = t; i < B.np; i += T) {
+      const uint32_t k = bidx[i];
+      gp[k] = sp[i];
+      if (FULL) gq[k] = sq[i];
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Serial executor: one thread replays one body's reference loops directly, in
+// insertion order (src/solver.rs:143-146, :155-158, :118-121).  Used for
+// chain-like bodies (rings, ropes) whose level schedule has width ~1, where a
+// whole group would idle.  Link endpoints are world indices.
+// ----------------------------------------------------------------------------
+template <bool FULL>
+__global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __restrict__ list,
+                              uint32_t n, uint32_t cur, uint32_t sub) {
+  const uint32_t it0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it0 >= n) return;
+  const uint2 wi = list[it0];
+  const DWorld& W = worlds[wi.x];
+  if (!FULL && sub >= W.S) return;
+  const DBody B = W.bodies[wi.y];
+  float2* p = W.pos[cur];
+  float2* q = W.prev;
+  const uint2* ab = W.lab + B.l0;
+  const float* rest = W.lrest + B.l0;
+  const float* stiff = W.lstiff + B.l0;
+  const uint32_t* bidx = W.bidx + B.i0;
+  const uint32_t nsub = FULL ? W.S : 1u, I = W.I;
+  const float gx = W.gx, gy = W.gy, h = W.h;
+  DWorld Wb;
+  Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+  for (uint32_t s = 0; s < nsub; ++s) {
+    for (uint32_t it = 0; it < I; ++it) {
+      for (uint32_t k = 0; k < B.nl; ++k) {
+        const uint2 e = ab[k];
+        float2 pa = p[e.x], pb = p[e.y];
+        link_solve(pa, pb, rest[k], stiff[k]);
+        p[e.x] = pa;
+        p[e.y] = pb;
+      }
+    }
+    if (FULL) {
+      for (uint32_t k = 0; k < B.np; ++k) {
+        const uint32_t j = bidx[k];
+        float2 pp = p[j], qq = q[j];
+        solve_bounds(pp, qq, Wb);
+        integrate(pp, qq, gx, gy, h);
+        p[j] = pp;
+        q[j] = qq;
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Rigid executor: the circles and polygons of one world per CTA.  The
+// reference's sequential pair loops (circle pairs i<j; polygon pairs i<j in
+// both directions) run speculatively: every remaining test of a window is
+// evaluated in parallel on the current state; the first test, in reference
+// order, that changes state is applied alone and evaluation resumes right
+// after it.  Tests before the first hit changed nothing, so the outcome is
+// the sequential one.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void calc_center(const float2* v, uint32_t n, float2& c) {
+  // Polygon::calc_center, src/polygon.rs:231-237: sequential sum from 0, / n
+  float cx = 0.0f, cy = 0.0f;
+  for (uint32_t i = 0; i < n; ++i) { cx = fadd(cx, v[i].x); cy = fadd(cy, v[i].y); }
+  c.x = fdiv(cx, (float)n);
+  c.y = fdiv(cy, (float)n);
+}
+
+// common::line_intersection, src/common.rs:3-26
+__device__ __forceinline__ bool line_intersection(float2 p1, float2 p2, float2 p3, float2 p4,
+                                                  float2& out) {
+  float s1x = fsub(p2.x, p1.x), s1y = fsub(p2.y, p1.y);
+  float s2x = fsub(p4.x, p3.x), s2y = fsub(p4.y, p3.y);
+  float d13x = fsub(p1.x, p3.x), d13y = fsub(p1.y, p3.y);
+  float den = fadd(fmul(-s2x, s1y), fmul(s1x, s2y));
+  float s = fdiv(fadd(fmul(-s1y, d13x), fmul(s1x, d13y)), den);
+  float t = fdiv(fsub(fmul(s2x, d13y), fmul(s2y, d13x)), den);
+  if (s >= 0.0f && s <= 1.0f && t >= 0.0f && t <= 1.0f) {
+    out.x = fadd(p1.x, fmul(t, s1x));
+    out.y = fadd(p1.y, fmul(t, s1y));
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ float2 normalize2(float x, float y) {
+  float n = fsqrt(norm_sq(x, y));
+  return make_float2(fdiv(x, n), fdiv(y, n));
+}
+
+// Polygon::resolve_line_intersection, src/polygon.rs:164-216
+__device__ bool resolve_line(float2 self_center, float2 pa, float2 pb, float2 q,
+                             float2 other_center, float2& na, float2& nb, float2& nq) {
+  float2 I;
+  if (!line_intersection(pa, pb, q, other_center, I)) return false;
+  float2 nl = normalize2(fsub(pb.x, pa.x), fsub(pb.y, pa.y));
+  float k = fdiv(dot2(nl.x, nl.y, fsub(self_center.x, I.x), fsub(self_center.y, I.y)),
+                 dot2(nl.x, nl.y, nl.x, nl.y));
+  float2 cp = make_float2(fmul(nl.x, k), fmul(nl.y, k));
+  float2 ni = normalize2(fsub(self_center.x, fadd(I.x, cp.x)), fsub(self_center.y, fadd(I.y, cp.y)));
+  float dax = fsub(I.x, pa.x), day = fsub(I.y, pa.y);
+  float dbx = fsub(I.x, pb.x), dby = fsub(I.y, pb.y);
+  float dist_a = fsqrt(norm_sq(dax, day));
+  float dist_b = fsqrt(norm_sq(dbx, dby));
+  float dab = fadd(dist_a, dist_b);
+  float inf_a = fdiv(dist_b, dab), inf_b = fdiv(dist_a, dab);
+  float dx = fsub(I.x, q.x), dy = fsub(I.y, q.y);
+  float kk = fdiv(dot2(ni.x, ni.y, dx, dy), dot2(ni.x, ni.y, ni.x, ni.y));
+  float onx = fmul(ni.x, kk), ony = fmul(ni.y, kk);
+  float lx = fmul(fdiv(onx, 3.0f), 2.0f), ly = fmul(fdiv(ony, 3.0f), 2.0f);
+  float2 a2 = make_float2(fsub(pa.x, fmul(lx, inf_a)), fsub(pa.y, fmul(ly, inf_a)));
+  float2 b2 = make_float2(fsub(pb.x, fmul(lx, inf_b)), fsub(pb.y, fmul(ly, inf_b)));
+  float2 far = make_float2(fsub(q.x, fmul(ni.x, 10000.0f)), fsub(q.y, fmul(ni.y, 10000.0f)));
+  float2 hit;
+  if (line_intersection(pa, pb, q, far, hit)) {
+    na = a2; nb = b2; nq = hit;
+    return true;
+  }
+  return false;
+}
+
+// Circle::solve_circle, src/circle.rs:32-45 (state-changing part)
+__device__ __forceinline__ bool circle_pair_hits(float2 pi, float ri, float2 pj, float rj) {
+  float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y);
+  float rs = fadd(ri, rj);
+  return norm_sq(dx, dy) < fmul(rs, rs);
+}
+__device__ __forceinline__ void circle_pair_apply(float2& pi, float ri, float2& pj, float rj) {
+  float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y);
+  float d2 = norm_sq(dx, dy);
+  float rs = fadd(ri, rj);
+  if (d2 < fmul(rs, rs)) {
+    float2 n = normalize2(dx, dy);
+    float overlap = fsub(rs, fsqrt(d2));
+    float ri2 = fmul(ri, ri), rj2 = fmul(rj, rj);
+    float scale = fdiv(1.0f, fadd(ri2, rj2));
+    pi.x = fadd(pi.x, fmul(fmul(fmul(n.x, scale), overlap), rj2));
+    pi.y = fadd(pi.y, fmul(fmul(fmul(n.y, scale), overlap), rj2));
+    pj.x = fsub(pj.x, fmul(fmul(fmul(n.x, scale), overlap), ri2));
+    pj.y = fsub(pj.y, fmul(fmul(fmul(n.y, scale), overlap), ri2));
+  }
+}
+
+// CircleLink::solve, src/link.rs:36-48
+__device__ __forceinline__ void circle_link_solve(float2& a, float ra, float2& b, float rb,
+                                                  float rest) {
+  float dx = fsub(a.x, b.x), dy = fsub(a.y, b.y);
+  float dist = fsqrt(norm_sq(dx, dy));
+  float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
+  float ra2 = fmul(ra, ra), rb2 = fmul(rb, rb);
+  float scale = fdiv(1.0f, fadd(ra2, rb2));
+  float m = fsub(dist, rest);
+  a.x = fsub(a.x, fmul(fmul(fmul(nx, m), scale), rb2));
+  a.y = fsub(a.y, fmul(fmul(fmul(ny, m), scale), rb2));
+  b.x = fadd(b.x, fmul(fmul(fmul(nx, m), scale), ra2));
+  b.y = fadd(b.y, fmul(fmul(fmul(ny, m), scale), ra2));
+}
+
+__device__ __forceinline__ uint64_t pair_row_off(uint64_t i, uint64_t n) {
+  return i * (2 * n - i - 1) / 2;
+}
+// k-th pair (i<j) in row-major order over n items
+__device__ __forceinline__ void unrank_pair(uint64_t k, uint32_t n, uint32_t& i, uint32_t& j) {
+  double dn = (double)n;
+  double disc = (2.0 * dn - 1.0) * (2.0 * dn - 1.0) - 8.0 * (double)k;
+  if (disc < 0.0) disc = 0.0;
+  int64_t x = (int64_t)((2.0 * dn - 1.0 - sqrt(disc)) * 0.5);
+  if (x < 0) x = 0;
+  if (x > (int64_t)n - 2) x = (int64_t)n - 2;
+  uint64_t ii = (uint64_t)x;
+  while (ii > 0 && pair_row_off(ii, n) > k) --ii;
+  while (ii + 1 < n && pair_row_off(ii + 1, n) <= k) ++ii;
+  i = (uint32_t)ii;
+  j = (uint32_t)(k - pair_row_off(ii, n) + ii + 1);
+}
+
+// Polygon pair "stages": stage s = (self, other) in reference order (pairs
+// i<j row-major; (i,j) then (j,i)).  Test x within a stage is (edge e of
+// self, point q of other), numbered e*nv_other + q.  The host stores
+// stage_off[s] = first test of stage s, and the total after the last stage.
+__device__ __forceinline__ void stage_pair(uint32_t s, uint32_t ng, uint32_t& self,
+                                           uint32_t& other) {
+  uint32_t i, j;
+  unrank_pair(s >> 1, ng, i, j);
+  if (s & 1) { self = j; other = i; } else { self = i; other = j; }
+}
+
+__device__ __forceinline__ uint32_t stage_of(const uint32_t* so, uint32_t nstage, uint32_t x) {
+  uint32_t lo = 0, hi = nstage;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (so[mid] <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// gravity + links + circle pairs + polygon pairs of one sub-step for the
+// circles and polygons (src/solver.rs:110-112)
+__device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  float2* cp = W.cpos;
+  float2* ca = W.cacc;
+  const float* cr = W.crad;
+  const DPoly* polys = W.polys;
+  __shared__ uint32_t s_first;
+  // gravity, src/solver.rs:130-141 (static bodies included)
+  for (uint32_t i = tid; i < W.nc; i += nt) {
+    float2 a = ca[i];
+    a.x = fadd(a.x, W.gx); a.y = fadd(a.y, W.gy);
+    ca[i] = a;
+  }
+  for (uint32_t g = 0; g < W.ng; ++g) {
+    const DPoly P = polys[g];
+    for (uint32_t v = tid; v < P.nv; v += nt) {
+      float2 a = W.vacc[P.v0 + v];
+      a.x = fadd(a.x, W.gx); a.y = fadd(a.y, W.gy);
+      W.vacc[P.v0 + v] = a;
+    }
+  }
+  __syncthreads();
+  // links, src/solver.rs:143-153, repeated I times (extension)
+  for (uint32_t it = 0; it < W.I; ++it) {
+    if (tid == 0) {
+      for (uint32_t k = 0; k < W.ncl; ++k) {
+        const uint2 e = W.clab[k];
+        float2 pa = cp[e.x], pb = cp[e.y];
+        circle_link_solve(pa, cr[e.x], pb, cr[e.y], W.clrest[k]);
+        cp[e.x] = pa; cp[e.y] = pb;
+      }
+    }
+    for (uint32_t g = tid; g < W.ng; g += nt) {  // one thread per polygon
+      const DPoly P = polys[g];
+      float2* v = W.vpos + P.v0;
+      float2 c;
+      calc_center(v, P.nv, c);  // Polygon::solve_links, src/polygon.rs:218-223
+      W.pcenter[g] = c;
+      for (uint32_t k = 0; k < P.nl; ++k) {
+        const uint2 e = W.plab[P.l0 + k];
+        float2 pa = v[e.x], pb = v[e.y];
+        link_solve(pa, pb, W.plrest[P.l0 + k], 1.0f);
+        v[e.x] = pa; v[e.y] = pb;
+      }
+    }
+    __syncthreads();
+  }
+  // circle pairs, src/solver.rs:168-177, speculative windows of nt pairs
+  {
+    const uint64_t npairs = W.nc >= 2 ? (uint64_t)W.nc * (W.nc - 1) / 2 : 0;
+    uint64_t start = 0;
+    while (start < npairs) {
+      if (tid == 0) s_first = 0xFFFFFFFFu;
+      __syncthreads();
+      const uint64_t k = start + tid;
+      if (k < npairs) {
+        uint32_t i, j;
+        unrank_pair(k, W.nc, i, j);
+        if (circle_pair_hits(cp[i], cr[i], cp[j], cr[j])) atomicMin(&s_first, tid);
+      }
+      __syncthreads();
+      const uint32_t f = s_first;
+      if (f == 0xFFFFFFFFu) {
+        start += nt;
+      } else {
+        if (tid == f) {
+          uint32_t i, j;
+          unrank_pair(k, W.nc, i, j);
+          float2 pi = cp[i], pj = cp[j];
+          circle_pair_apply(pi, cr[i], pj, cr[j]);
+          cp[i] = pi; cp[j] = pj;
+        }
+        start += f + 1;
+      }
+      __syncthreads();
+    }
+  }
+  // polygon pairs, src/solver.rs:178-187 + src/polygon.rs:142-216
+  const uint32_t nstage = W.ng >= 2 ? W.ng * (W.ng - 1) : 0;
+  if (nstage > 0) {
+    const uint32_t* so = W.stage_off;
+    const uint32_t total = so[nstage];
+    uint32_t start = 0;
+    while (start < total) {
+      if (tid == 0) s_first = 0xFFFFFFFFu;
+      __syncthreads();
+      const uint32_t x = start + tid;
+      if (x < total) {
+        const uint32_t st = stage_of(so, nstage, x);
+        uint32_t self, other;
+        stage_pair(st, W.ng, self, other);
+        const DPoly PS = polys[self], PO = polys[other];
+        const uint32_t r = x - so[st];
+        const uint32_t e = r / PO.nv;
+        const uint32_t q = r - e * PO.nv;
+        const uint32_t b = (e + 1) % PS.nv;
+        float2 na, nb, nq;
+        if (resolve_line(W.pcenter[self], W.vpos[PS.v0 + e], W.vpos[PS.v0 + b],
+                         W.vpos[PO.v0 + q], W.pcenter[other], na, nb, nq))
+          atomicMin(&s_first, x);
+      }
+      __syncthreads();
+      const uint32_t f = s_first;
+      __syncthreads();
+      if (f == 0xFFFFFFFFu) {
+        start += nt;
+        continue;
+      }
+      // Apply the whole edge step holding test f: every point of `other`, in
+      // order.  The edge endpoints are copies taken before the point loop, so
+      // the last hit sets them (src/polygon.rs:148-160).
+      if (tid == 0) {
+        const uint32_t st = stage_of(so, nstage, f);
+        uint32_t self, other;
+        stage_pair(st, W.ng, self, other);
+        const DPoly PS = polys[self], PO = polys[other];
+        const uint32_t e = (f - so[st]) / PO.nv;
+        const uint32_t b = (e + 1) % PS.nv;
+        const float2 pa = W.vpos[PS.v0 + e], pb = W.vpos[PS.v0 + b];
+        const float2 sc = W.pcenter[self], oc = W.pcenter[other];
+        for (uint32_t q = 0; q < PO.nv; ++q) {
+          float2 na, nb, nq;
+          if (resolve_line(sc, pa, pb, W.vpos[PO.v0 + q], oc, na, nb, nq)) {
+            W.vpos[PS.v0 + e] = na;
+            W.vpos[PS.v0 + b] = nb;
+            W.vpos[PO.v0 + q] = nq;
+          }
+        }
+        s_first = so[st] + (e + 1) * PO.nv;  // first test of the next edge step
+      }
+      __syncthreads();
+      start = s_first;
+      __syncthreads();
+    }
+  }
+  // extension: polygon vertex bounding boxes for particle-polygon contacts
+  if (want_aabb) {
+    for (uint32_t g = tid; g < W.ng; g += nt) {
+      const DPoly P = polys[g];
+      const float2* v = W.vpos + P.v0;
+      float4 bb = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (P.nv > 0) {
+        bb = make_float4(v[0].x, v[0].y, v[0].x, v[0].y);
+        for (uint32_t i = 1; i < P.nv; ++i) {
+          if (v[i].x < bb.x) bb.x = v[i].x;
+          if (v[i].y < bb.y) bb.y = v[i].y;
+          if (v[i].x > bb.z) bb.z = v[i].x;
+          if (v[i].y > bb.w) bb.w = v[i].y;
+        }
+      }
+      W.paabb[g] = bb;
+    }
+  }
+  __syncthreads();
+}
+
+// bounds + integrate of one sub-step for the circles and polygons
+// (src/solver.rs:113-114)
+__device__ void rigid_phase_b(const DWorld& W) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  float2* cp = W.cpos;
+  float2* cq = W.cprev;
+  float2* ca = W.cacc;
+  const float* cr = W.crad;
+  const DPoly* polys = W.polys;
+  // bounds, src/solver.rs:155-165
+  for (uint32_t i = tid; i < W.nc; i += nt) {
+    float2 p = cp[i], q = cq[i];
+    circle_bounds(p, q, cr[i], W);
+    cp[i] = p; cq[i] = q;
+  }
+  for (uint32_t g = 0; g < W.ng; ++g) {
+    const DPoly P = polys[g];
+    for (uint32_t v = tid; v < P.nv; v += nt) {
+      float2 p = W.vpos[P.v0 + v], q = W.vprev[P.v0 + v];
+      solve_bounds(p, q, W);
+      W.vpos[P.v0 + v] = p; W.vprev[P.v0 + v] = q;
+    }
+  }
+  __syncthreads();
+  // update_positions, src/solver.rs:118-128
+  for (uint32_t i = tid; i < W.nc; i += nt) {
+    if (W.cstatic[i]) continue;  // extension: static circle
+    float2 p = cp[i], q = cq[i];
+    const float2 a = ca[i];
+    integrate(p, q, a.x, a.y, W.h);
+    cp[i] = p; cq[i] = q; ca[i] = make_float2(0.0f, 0.0f);
+  }
+  for (uint32_t g = tid; g < W.ng; g += nt) {  // Polygon::update, src/polygon.rs:125-134
+    const DPoly P = polys[g];
+    if (P.is_static) continue;
+    float2 c;
+    calc_center(W.vpos + P.v0, P.nv, c);
+    W.pcenter[g] = c;
+  }
+  __syncthreads();
+  for (uint32_t g = 0; g < W.ng; ++g) {
+    const DPoly P = polys[g];
+    if (P.is_static) continue;
+    for (uint32_t v = tid; v < P.nv; v += nt) {
+      float2 p = W.vpos[P.v0 + v], q = W.vprev[P.v0 + v];
+      const float2 a = W.vacc[P.v0 + v];
+      integrate(p, q, a.x, a.y, W.h);
+      W.vpos[P.v0 + v] = p; W.vprev[P.v0 + v] = q;
+      W.vacc[P.v0 + v] = make_float2(0.0f, 0.0f);
+    }
+  }
+  __syncthreads();
+}
+
+// MODE 0: the whole Solver::update step; 1: phase A of sub-step `sub`;
+// 2: phase B of sub-step `sub`; 3: phase B of `sub`-1, then phase A of `sub`.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_rigid(const DWorld* __restrict__ worlds,
+                                               const uint32_t* __restrict__ wlist, uint32_t n,
+                                               uint32_t sub) {
+  if (blockIdx.x >= n) return;
+  const DWorld& W = worlds[wlist[blockIdx.x]];
+  const bool aabb = (W.flags & COLLIDE_PPOLY) != 0;
+  if (MODE == 0) {
+    for (uint32_t s = 0; s < W.S; ++s) {
+      rigid_phase_a(W, false);
+      rigid_phase_b(W);
+    }
+  } else if (MODE == 1) {
+    if (sub < W.S) rigid_phase_a(W, aabb);
+  } else if (MODE == 2) {
+    if (sub < W.S) rigid_phase_b(W);
+  } else {
+    if (sub >= 1 && sub - 1 < W.S) rigid_phase_b(W);
+    if (sub < W.S) rigid_phase_a(W, aabb);
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Extension: particle collisions (not in the reference, whose solver
+// particles only interact through links, src/solver.rs:143-188).  Hashed
+// uniform grid: bucket = hash(world, cell) & mask with BUCKET_K slots per
+// bucket plus an overflow list.  For each particle, neighbour cells are
+// visited dy outer, dx inner (-1..1) and, within a cell, particles in
+// ascending index: the Jacobi sum order is fixed by the spec, not by hashing
+// or by the order of atomics.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell) {
+  float v = floorf(fdiv(fsub(p, origin), cell));
+  if (!(v > -1.0e9f)) v = -1.0e9f;
+  if (v > 1.0e9f) v = 1.0e9f;
+  return (int32_t)v;
+}
+__device__ __forceinline__ uint32_t cell_hash(uint32_t w, int32_t cx, int32_t cy, uint32_t mask) {
+  uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ (w * 83492791u);
+  h ^= h >> 15;
+  h *= 0x2c1b3c6du;
+  h ^= h >> 12;
+  return h & mask;
+}
+
+constexpr uint32_t CHUNK = 256;  // particles per work chunk (one CTA)
+
+__global__ void __launch_bounds__(CHUNK) k_grid_insert(const DWorld* __restrict__ worlds, DGrid G,
+                                                       const uint2* __restrict__ chunks,
+                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
+  if (blockIdx.x >= nchunks) return;
+  const uint2 ch = chunks[blockIdx.x];
+  const DWorld& W = worlds[ch.x];
+  const uint32_t j = ch.y + threadIdx.x;
+  if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
+  const float2 p = W.pos[cur][j];
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
+  const uint32_t b = cell_hash(ch.x, cx, cy, G.mask);
+  const uint32_t s = atomicAdd(&G.count[b], 1u);
+  const uint4 ent = make_uint4(ch.x, j, (uint32_t)cx, (uint32_t)cy);
+  if (s < BUCKET_K) {
+    G.slots[(size_t)b * BUCKET_K + s] = ent;
+  } else {
+    const uint32_t o = atomicAdd(&G.ovf_n[0], 1u);
+    if (o < G.ovf_cap) {  // capacity = all particles, so this always holds
+      G.overflow[o] = ent;
+      G.ovf_bucket[o] = b;
+    }
+  }
+}
+
+__device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D2, float& ddx,
+                                           float& ddy, bool& hit) {
+  const float dx = fsub(p.x, pj.x), dy = fsub(p.y, pj.y);
+  const float d2 = fadd(fmul(dx, dx), fmul(dy, dy));
+  if (d2 < D2 && d2 > 0.0f) {
+    const float dist = fsqrt(d2);
+    const float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
+    const float ov = fsub(D, dist);
+    ddx = fadd(ddx, fmul(fmul(nx, ov), 0.5f));
+    ddy = fadd(ddy, fmul(fmul(ny, ov), 0.5f));
+    hit = true;
+  }
+}
+
+// particle-Circle (circles are kinematic for particles; index order)
+__device__ float2 particle_circles(const DWorld& W, float2 p) {
+  for (uint32_t k = 0; k < W.nc; ++k) {
+    const float2 c = W.cpos[k];
+    const float dx = fsub(p.x, c.x), dy = fsub(p.y, c.y);
+    const float d2 = fadd(fmul(dx, dx), fmul(dy, dy));
+    const float R = fadd(W.radius, W.crad[k]);
+    if (d2 < fmul(R, R) && d2 > 0.0f) {
+      const float dist = fsqrt(d2);
+      const float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
+      const float m = fsub(R, dist);
+      p.x = fadd(p.x, fmul(nx, m));
+      p.y = fadd(p.y, fmul(ny, m));
+    }
+  }
+  return p;
+}
+
+// particle-Polygon edge projection (one-way)
+__device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p) {
+  const DPoly P = W.polys[k];
+  if (P.nv < 3) return p;
+  const float4 bb = W.paabb[k];
+  const float r = W.radius;
+  if (!(p.x >= fsub(bb.x, r) && p.x <= fadd(bb.z, r) && p.y >= fsub(bb.y, r) &&
+        p.y <= fadd(bb.w, r)))
+    return p;
+  const float2* v = W.vpos + P.v0;
+  bool inside = false;
+  float best = __int_as_float(0x7f800000);
+  float2 bq = p;
+  for (uint32_t e = 0; e < P.nv; ++e) {
+    const float2 a = v[e];
+    const float2 b = v[e + 1 == P.nv ? 0 : e + 1];
+    if ((a.y > p.y) != (b.y > p.y)) {
+      const float t = fdiv(fsub(p.y, a.y), fsub(b.y, a.y));
+      const float xint = fadd(a.x, fmul(t, fsub(b.x, a.x)));
+      if (p.x < xint) inside = !inside;
+    }
+    const float abx = fsub(b.x, a.x), aby = fsub(b.y, a.y);
+    const float l2 = fadd(fmul(abx, abx), fmul(aby, aby));
+    float t = 0.0f;
+    if (l2 > 0.0f) t = fdiv(fadd(fmul(fsub(p.x, a.x), abx), fmul(fsub(p.y, a.y), aby)), l2);
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    const float qx = fadd(a.x, fmul(abx, t)), qy = fadd(a.y, fmul(aby, t));
+    const float dqx = fsub(p.x, qx), dqy = fsub(p.y, qy);
+    const float d2 = fadd(fmul(dqx, dqx), fmul(dqy, dqy));
+    if (d2 < best) { best = d2; bq = make_float2(qx, qy); }
+  }
+  if (inside) {
+    const float dist = fsqrt(best);
+    if (dist > 0.0f) {
+      const float nx = fdiv(fsub(bq.x, p.x), dist), ny = fdiv(fsub(bq.y, p.y), dist);
+      return make_float2(fadd(bq.x, fmul(nx, r)), fadd(bq.y, fmul(ny, r)));
+    }
+    return bq;
+  }
+  if (best < fmul(r, r)) {
+    const float dist = fsqrt(best);
+    if (dist > 0.0f) {
+      const float nx = fdiv(fsub(p.x, bq.x), dist), ny = fdiv(fsub(p.y, bq.y), dist);
+      return make_float2(fadd(bq.x, fmul(nx, r)), fadd(bq.y, fmul(ny, r)));
+    }
+  }
+  return p;
+}
+
+// Particle collisions + bounds + integrate of one sub-step of the extension
+// pipeline.  Reads positions from buffer cur (the post-link snapshot) and
+// writes the new ones to buffer cur^1; prev is updated in place.
+__global__ void __launch_bounds__(CHUNK) k_collide_integrate(const DWorld* __restrict__ worlds,
+                                                             DGrid G, const uint2* __restrict__ chunks,
+                                                             uint32_t nchunks, uint32_t cur,
+                                                             uint32_t sub) {
+  if (blockIdx.x >= nchunks) return;
+  const uint2 ch = chunks[blockIdx.x];
+  const DWorld& W = worlds[ch.x];
+  const uint32_t i = ch.y + threadIdx.x;
+  if (i >= W.np || sub >= W.S) return;
+  const float2* P = W.pos[cur];
+  float2 p = P[i];
+  float2 q = W.prev[i];
+  if (W.flags & COLLIDE_PP) {
+    const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
+    const float D = fadd(W.radius, W.radius);
+    const float D2 = fmul(D, D);
+    const uint32_t novf = min(G.ovf_n[0], G.ovf_cap);
+    float ddx = 0.0f, ddy = 0.0f;
+    bool hit = false;
+    for (int dy = -1; dy <= 1; ++dy) {
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int32_t ncx = cx + dx, ncy = cy + dy;
+        const uint32_t b = cell_hash(ch.x, ncx, ncy, G.mask);
+        const uint32_t cnt = G.count[b];
+        if (cnt == 0) continue;
+        const uint32_t nk = cnt < BUCKET_K ? cnt : BUCKET_K;
+        const uint4* sl = G.slots + (size_t)b * BUCKET_K;
+        // matching entries in ascending particle index (selection order)
+        uint32_t last = 0;
+        bool have_last = false;
+        for (;;) {
+          uint32_t best = 0xFFFFFFFFu;
+          for (uint32_t s = 0; s < nk; ++s) {
+            const uint4 e = sl[s];
+            if (e.x != ch.x || (int32_t)e.z != ncx || (int32_t)e.w != ncy) continue;
+            if (have_last && e.y <= last) continue;
+            if (e.y < best) best = e.y;
+          }
+          if (cnt > BUCKET_K) {
+            for (uint32_t o = 0; o < novf; ++o) {
+              if (G.ovf_bucket[o] != b) continue;
+              const uint4 e = G.overflow[o];
+              if (e.x != ch.x || (int32_t)e.z != ncx || (int32_t)e.w != ncy) continue;
+              if (have_last && e.y <= last) continue;
+              if (e.y < best) best = e.y;
+            }
+          }
+          if (best == 0xFFFFFFFFu) break;
+          last = best;
+          have_last = true;
+          if (best == i) continue;
+          pp_contact(p, P[best], D, D2, ddx, ddy, hit);
+        }
+      }
+    }
+    if (hit) { p.x = fadd(p.x, ddx); p.y = fadd(p.y, ddy); }
+  }
+  if (W.flags & COLLIDE_PC) p = particle_circles(W, p);
+  if (W.flags & COLLIDE_PPOLY) {
+    for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
+  }
+  solve_bounds(p, q, W);
+  integrate(p, q, W.gx, W.gy, W.h);
+  W.pos[cur ^ 1u][i] = p;
+  W.prev[i] = q;
+}
+
+// positions of worlds whose step ended in buffer 1 go back to buffer 0
+__global__ void __launch_bounds__(CHUNK) k_copy_back(const DWorld* __restrict__ worlds,
+                                                     const uint2* __restrict__ chunks,
+                                                     uint32_t nchunks) {
+  if (blockIdx.x >= nchunks) return;
+  const uint2 ch = chunks[blockIdx.x];
+  const DWorld& W = worlds[ch.x];
+  const uint32_t i = ch.y + threadIdx.x;
+  if (i >= W.np || !(W.S & 1u)) return;
+  W.pos[0][i] = W.pos[1][i];
+}
+
+}  // namespace b2d

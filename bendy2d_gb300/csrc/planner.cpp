@@ -1,0 +1,403 @@
+// planner.cpp — turns one world (the reference's Solver contents) into its
+// device image: bodies, executor choice, level schedules and the world block.
+//
+// Level scheduling.  The reference applies links one at a time in insertion
+// order (src/solver.rs:143-146), then bounds and integration per particle
+// (src/solver.rs:155-158, :118-121).  Give each op the level
+//   level(op) = 1 + max(level of the last earlier op touching any of its particles)
+// Ops on one level touch disjoint particles, and every particle sees its ops
+// in the original order, so executing level by level reproduces the
+// sequential loop exactly.  A FULL schedule chains all sub-steps and link
+// iterations of one Solver::update, which lets independent regions of a body
+// run ahead into later passes (the critical path of a 32x32 cloth step drops
+// from 4032 to ~413 levels).
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#include "engine.hpp"
+
+namespace b2d {
+
+static uint32_t pow2ceil(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I,
+                            bool full) {
+  std::string key;
+  key.resize(20 + (size_t)nl * 8);
+  const uint32_t hdr[5] = {np, nl, S, I, full ? 1u : 0u};
+  std::memcpy(&key[0], hdr, 20);
+  if (nl) std::memcpy(&key[20], links, (size_t)nl * 8);
+  auto it = index.find(key);
+  if (it != index.end()) return it->second;
+
+  const uint32_t nsub = full ? S : 1u;
+  const size_t total = (size_t)nsub * ((size_t)I * nl + (full ? np : 0));
+  std::vector<uint32_t> last(np, 0), lvl_of, op_of;
+  lvl_of.reserve(total);
+  op_of.reserve(total);
+  uint32_t maxl = 0;
+  for (uint32_t s = 0; s < nsub; ++s) {
+    for (uint32_t it2 = 0; it2 < I; ++it2) {
+      for (uint32_t k = 0; k < nl; ++k) {
+        const uint32_t a = links[k].x, b = links[k].y;
+        const uint32_t l = std::max(last[a], last[b]) + 1;
+        last[a] = l;
+        last[b] = l;
+        lvl_of.push_back(l);
+        op_of.push_back(k);
+        maxl = std::max(maxl, l);
+      }
+    }
+    if (full) {
+      for (uint32_t p = 0; p < np; ++p) {
+        const uint32_t l = last[p] + 1;
+        last[p] = l;
+        lvl_of.push_back(l);
+        op_of.push_back(OP_INTEG | p);
+        maxl = std::max(maxl, l);
+      }
+    }
+  }
+  // stable counting sort by level
+  std::vector<uint32_t> start(maxl + 2, 0);
+  for (uint32_t l : lvl_of) start[l + 1]++;
+  for (uint32_t l = 1; l <= maxl + 1; ++l) start[l] += start[l - 1];
+  DSched d;
+  d.lvl0 = (uint32_t)lvl.size();
+  d.nlvl = maxl;
+  d.op0 = (uint32_t)ops.size();
+  d.nops = (uint32_t)total;
+  for (uint32_t l = 1; l <= maxl + 1; ++l) lvl.push_back(start[l]);  // lv[l-1] = begin of level l
+  ops.resize(ops.size() + total);
+  uint32_t* dst = ops.data() + d.op0;
+  std::vector<uint32_t> fill(start.begin(), start.end());
+  for (size_t i = 0; i < total; ++i) dst[fill[lvl_of[i]]++] = op_of[i];
+  const uint32_t id = (uint32_t)scheds.size();
+  scheds.push_back(d);
+  index.emplace(std::move(key), id);
+  return id;
+}
+
+namespace {
+struct Comp {
+  std::vector<uint32_t> parts;  // ascending world indices
+  std::vector<uint32_t> links;  // world link ids in execution order
+};
+
+uint32_t single_pass_depth(const WorldHost& w, const Comp& c, std::vector<uint32_t>& last) {
+  uint32_t depth = 0;
+  for (uint32_t k : c.links) {
+    const uint32_t a = (uint32_t)w.particle_links[k].particle_a;
+    const uint32_t b = (uint32_t)w.particle_links[k].particle_b;
+    const uint32_t l = std::max(last[a], last[b]) + 1;
+    last[a] = l;
+    last[b] = l;
+    depth = std::max(depth, l);
+  }
+  for (uint32_t k : c.links) {
+    last[w.particle_links[k].particle_a] = 0;
+    last[w.particle_links[k].particle_b] = 0;
+  }
+  return depth;
+}
+}  // namespace
+
+int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, WorldImage& im,
+               std::string* why) {
+  int st = validate_world(w, why);
+  if (st != OK) return st;
+  const size_t np64 = w.particles.size();
+  if (np64 >= 0x7FFFFFFFull || w.particle_links.size() >= 0x7FFFFFFFull) {
+    if (why) *why = "world too large for 32-bit indices";
+    return ERR_ARG;
+  }
+  const uint32_t np = (uint32_t)np64;
+  const uint32_t nl = (uint32_t)w.particle_links.size();
+  im = WorldImage();
+  DWorld& P = im.params;
+  std::memset(&P, 0, sizeof(P));
+  P.gx = 0.0f + w.gravity.x;  // acc = 0 + g at integrate time (src/particle.rs:52-54)
+  P.gy = 0.0f + w.gravity.y;
+  P.bx = w.bounds.pos.x;
+  P.by = w.bounds.pos.y;
+  P.bw = w.bounds.size.x;
+  P.bh = w.bounds.size.y;
+  P.radius = w.particle_radius;
+  P.cell = w.grid_cell;
+  P.S = w.sub_steps;
+  P.I = w.link_iters;
+  P.flags = w.collide & (COLLIDE_PP | COLLIDE_PC | COLLIDE_PPOLY);
+  P.np = np;
+  P.nc = (uint32_t)w.circles.size();
+  P.ncl = (uint32_t)w.circle_links.size();
+  P.ng = (uint32_t)w.polygons.size();
+  im.ext = P.flags != 0;
+  const bool full = !im.ext;
+
+  im.pos.resize(np);
+  im.prev.resize(np);
+  for (uint32_t i = 0; i < np; ++i) {
+    im.pos[i] = make_float2(w.particles[i].pos.x, w.particles[i].pos.y);
+    im.prev[i] = make_float2(w.particles[i].prev_pos.x, w.particles[i].prev_pos.y);
+  }
+
+  // link execution order: insertion order, or colour-major in fast mode
+  std::vector<uint32_t> order(nl);
+  std::iota(order.begin(), order.end(), 0u);
+  if (w.mode == MODE_FAST) {
+    order = colour_link_order(w, &im.stats.colours);
+    im.link_order = order;
+  }
+
+  // connected components (union-find over links)
+  std::vector<uint32_t> parent(np);
+  std::iota(parent.begin(), parent.end(), 0u);
+  auto find = [&](uint32_t x) {
+    while (parent[x] != x) {
+      parent[x] = parent[parent[x]];
+      x = parent[x];
+    }
+    return x;
+  };
+  for (uint32_t k = 0; k < nl; ++k) {
+    uint32_t a = find((uint32_t)w.particle_links[k].particle_a);
+    uint32_t b = find((uint32_t)w.particle_links[k].particle_b);
+    if (a != b) parent[std::max(a, b)] = std::min(a, b);
+  }
+  std::vector<int64_t> comp_of_root(np, -1);
+  std::vector<Comp> comps;
+  std::vector<uint32_t> comp_of(np);
+  for (uint32_t i = 0; i < np; ++i) {
+    const uint32_t r = find(i);
+    if (comp_of_root[r] < 0) {
+      comp_of_root[r] = (int64_t)comps.size();
+      comps.emplace_back();
+    }
+    comp_of[i] = (uint32_t)comp_of_root[r];
+    comps[comp_of[i]].parts.push_back(i);
+  }
+  for (uint32_t k : order) comps[comp_of[w.particle_links[k].particle_a]].links.push_back(k);
+
+  std::vector<uint32_t> last(np, 0), local(np, 0);
+  std::vector<uint32_t> free_parts;
+  std::vector<const Comp*> pack;
+  uint32_t pack_np = 0, pack_nl = 0;
+
+  auto emit_group = [&](const std::vector<const Comp*>& cs) {
+    DBody B{};
+    B.i0 = (uint32_t)im.bidx.size();
+    B.l0 = (uint32_t)im.lab.size();
+    uint32_t n = 0;
+    for (const Comp* c : cs)
+      for (uint32_t p : c->parts) {
+        local[p] = n++;
+        im.bidx.push_back(p);
+      }
+    B.np = n;
+    std::vector<uint2> loc;
+    for (const Comp* c : cs)
+      for (uint32_t k : c->links) {
+        const Link& L = w.particle_links[k];
+        loc.push_back(make_uint2(local[L.particle_a], local[L.particle_b]));
+        im.lrest.push_back(L.target_distance);
+        im.lstiff.push_back(L.stiffness);
+      }
+    B.nl = (uint32_t)loc.size();
+    B.sched = reg.get(loc.data(), B.nl, B.np, P.S, P.I, full);
+    const DSched& S = reg.scheds[B.sched];
+    const float avg = S.nlvl ? (float)S.nops / (float)S.nlvl : 1.0f;
+    uint32_t T = pow2ceil((uint32_t)(avg / tune.width_per_thread + 0.999f));
+    T = std::min(std::max(T, tune.t_min), tune.t_max);
+    const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 12u * (size_t)B.nl);
+    const bool smem = region <= tune.smem_max && B.np <= 65535u;
+    B.local = smem ? 1u : 0u;
+    for (size_t i = 0; i < loc.size(); ++i) {
+      if (smem) im.lab.push_back(loc[i]);
+      else im.lab.push_back(make_uint2(im.bidx[B.i0 + loc[i].x], im.bidx[B.i0 + loc[i].y]));
+    }
+    const uint32_t id = (uint32_t)im.bodies.size();
+    im.bodies.push_back(B);
+    im.groups.push_back(GroupBody{id, T, smem ? (uint32_t)region : 0u, smem});
+    im.stats.group_bodies++;
+    if (!smem) im.stats.global_bodies++;
+    im.stats.levels += S.nlvl;
+    im.stats.ops += S.nops;
+  };
+  auto flush_pack = [&]() {
+    if (!pack.empty()) emit_group(pack);
+    pack.clear();
+    pack_np = pack_nl = 0;
+  };
+
+  for (const Comp& c : comps) {
+    if (c.links.empty()) {
+      free_parts.push_back(c.parts[0]);
+      continue;
+    }
+    const uint32_t depth = single_pass_depth(w, c, last);
+    const float width = (float)c.links.size() / (float)std::max(depth, 1u);
+    if (width < tune.serial_width) {
+      DBody B{};
+      B.i0 = (uint32_t)im.bidx.size();
+      B.np = (uint32_t)c.parts.size();
+      B.l0 = (uint32_t)im.lab.size();
+      B.nl = (uint32_t)c.links.size();
+      B.local = 0;
+      for (uint32_t p : c.parts) im.bidx.push_back(p);
+      for (uint32_t k : c.links) {
+        const Link& L = w.particle_links[k];
+        im.lab.push_back(make_uint2((uint32_t)L.particle_a, (uint32_t)L.particle_b));
+        im.lrest.push_back(L.target_distance);
+        im.lstiff.push_back(L.stiffness);
+      }
+      im.serials.push_back((uint32_t)im.bodies.size());
+      im.bodies.push_back(B);
+      im.stats.serial_bodies++;
+      continue;
+    }
+    const uint32_t cn = (uint32_t)c.parts.size(), cl = (uint32_t)c.links.size();
+    if (!pack.empty() && (pack_np + cn > tune.pack_np || pack_nl + cl > tune.pack_nl)) flush_pack();
+    pack.push_back(&c);
+    pack_np += cn;
+    pack_nl += cl;
+  }
+  flush_pack();
+  // link-free particles: integrate-only bodies (the extension pipeline
+  // integrates every particle in its collide pass instead)
+  if (full) {
+    for (size_t i = 0; i < free_parts.size(); i += tune.free_chunk) {
+      std::vector<Comp> chunk(1);
+      const size_t e = std::min(free_parts.size(), i + tune.free_chunk);
+      chunk[0].parts.assign(free_parts.begin() + i, free_parts.begin() + e);
+      std::vector<const Comp*> cs{&chunk[0]};
+      emit_group(cs);
+    }
+  }
+  P.nb = (uint32_t)im.bodies.size();
+  im.stats.bodies = P.nb;
+
+  // circles (src/circle.rs:4-8) and circle links
+  for (const Circle& c : w.circles) {
+    im.cpos.push_back(make_float2(c.point.pos.x, c.point.pos.y));
+    im.cprev.push_back(make_float2(c.point.prev_pos.x, c.point.prev_pos.y));
+    im.cacc.push_back(make_float2(c.point.acc.x, c.point.acc.y));
+    im.crad.push_back(c.radius);
+    im.cstatic.push_back(c.is_static ? 1u : 0u);
+  }
+  for (const Link& l : w.circle_links) {
+    im.clab.push_back(make_uint2((uint32_t)l.particle_a, (uint32_t)l.particle_b));
+    im.clrest.push_back(l.target_distance);
+  }
+  // polygons (src/polygon.rs:7-14)
+  for (const Polygon& g : w.polygons) {
+    DPoly d{};
+    d.v0 = (uint32_t)im.vpos.size();
+    d.nv = (uint32_t)g.particles.size();
+    d.l0 = (uint32_t)im.plab.size();
+    d.nl = (uint32_t)g.particle_links.size();
+    d.is_static = g.is_static ? 1u : 0u;
+    for (const Particle& v : g.particles) {
+      im.vpos.push_back(make_float2(v.pos.x, v.pos.y));
+      im.vprev.push_back(make_float2(v.prev_pos.x, v.prev_pos.y));
+      im.vacc.push_back(make_float2(v.acc.x, v.acc.y));
+    }
+    for (const Link& l : g.particle_links) {
+      im.plab.push_back(make_uint2((uint32_t)l.particle_a, (uint32_t)l.particle_b));
+      im.plrest.push_back(l.target_distance);
+    }
+    im.pcenter.push_back(make_float2(g.center.x, g.center.y));
+    im.polys.push_back(d);
+  }
+  // polygon pair stages: (i,j) then (j,i) for pairs i<j in row-major order
+  if (P.ng >= 2) {
+    uint32_t acc = 0;
+    for (uint32_t i = 0; i < P.ng; ++i)
+      for (uint32_t j = i + 1; j < P.ng; ++j) {
+        im.stage_off.push_back(acc);
+        acc += im.polys[i].nv * im.polys[j].nv;
+        im.stage_off.push_back(acc);
+        acc += im.polys[j].nv * im.polys[i].nv;
+      }
+    im.stage_off.push_back(acc);
+  }
+  return OK;
+}
+
+BlockLayout layout_of(const WorldImage& im) {
+  BlockLayout L;
+  size_t o = 0;
+  auto seg = [&](size_t bytes) {
+    size_t at = o;
+    o = align16(o + bytes);
+    return at;
+  };
+  const size_t np = im.pos.size(), nc = im.cpos.size(), nv = im.vpos.size(),
+               ng = im.polys.size();
+  // the state prefix is one contiguous run of float2
+  L.o_pos = 0;
+  L.o_prev = L.o_pos + 8 * np;
+  L.o_cpos = L.o_prev + 8 * np;
+  L.o_cprev = L.o_cpos + 8 * nc;
+  L.o_cacc = L.o_cprev + 8 * nc;
+  L.o_vpos = L.o_cacc + 8 * nc;
+  L.o_vprev = L.o_vpos + 8 * nv;
+  L.o_vacc = L.o_vprev + 8 * nv;
+  L.o_pcenter = L.o_vacc + 8 * nv;
+  L.state_bytes = L.o_pcenter + 8 * ng;
+  o = align16(L.state_bytes);
+  L.o_pos1 = seg(8 * np);
+  L.o_bidx = seg(4 * im.bidx.size());
+  L.o_bodies = seg(sizeof(DBody) * im.bodies.size());
+  L.o_lab = seg(8 * im.lab.size());
+  L.o_lrest = seg(4 * im.lrest.size());
+  L.o_lstiff = seg(4 * im.lstiff.size());
+  L.o_crad = seg(4 * nc);
+  L.o_cstatic = seg(4 * nc);
+  L.o_clab = seg(8 * im.clab.size());
+  L.o_clrest = seg(4 * im.clrest.size());
+  L.o_polys = seg(sizeof(DPoly) * ng);
+  L.o_paabb = seg(16 * ng);
+  L.o_plab = seg(8 * im.plab.size());
+  L.o_plrest = seg(4 * im.plrest.size());
+  L.o_stage = seg(4 * im.stage_off.size());
+  L.total = std::max<size_t>(o, 16);
+  return L;
+}
+
+void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst) {
+  std::memset(dst, 0, L.total);
+  auto put = [&](size_t off, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(dst + off, src, bytes);
+  };
+  put(L.o_pos, im.pos.data(), 8 * im.pos.size());
+  put(L.o_prev, im.prev.data(), 8 * im.prev.size());
+  put(L.o_cpos, im.cpos.data(), 8 * im.cpos.size());
+  put(L.o_cprev, im.cprev.data(), 8 * im.cprev.size());
+  put(L.o_cacc, im.cacc.data(), 8 * im.cacc.size());
+  put(L.o_vpos, im.vpos.data(), 8 * im.vpos.size());
+  put(L.o_vprev, im.vprev.data(), 8 * im.vprev.size());
+  put(L.o_vacc, im.vacc.data(), 8 * im.vacc.size());
+  put(L.o_pcenter, im.pcenter.data(), 8 * im.pcenter.size());
+  put(L.o_pos1, im.pos.data(), 8 * im.pos.size());
+  put(L.o_bidx, im.bidx.data(), 4 * im.bidx.size());
+  put(L.o_bodies, im.bodies.data(), sizeof(DBody) * im.bodies.size());
+  put(L.o_lab, im.lab.data(), 8 * im.lab.size());
+  put(L.o_lrest, im.lrest.data(), 4 * im.lrest.size());
+  put(L.o_lstiff, im.lstiff.data(), 4 * im.lstiff.size());
+  put(L.o_crad, im.crad.data(), 4 * im.crad.size());
+  put(L.o_cstatic, im.cstatic.data(), 4 * im.cstatic.size());
+  put(L.o_clab, im.clab.data(), 8 * im.clab.size());
+  put(L.o_clrest, im.clrest.data(), 4 * im.clrest.size());
+  put(L.o_polys, im.polys.data(), sizeof(DPoly) * im.polys.size());
+  put(L.o_plab, im.plab.data(), 8 * im.plab.size());
+  put(L.o_plrest, im.plrest.data(), 4 * im.plrest.size());
+  put(L.o_stage, im.stage_off.data(), 4 * im.stage_off.size());
+}
+
+}  // namespace b2d

@@ -1,0 +1,174 @@
+/*
+ * bendy2d.h — C ABI of bendy2d-gb300, a GB300 (sm_103a) implementation of
+ * the Murrent/bendy2d 0.0.1 solver step.
+ *
+ * Every entry point returns an int status (B2D_OK = 0); b2d_last_error()
+ * gives a message for the last failure on the calling thread.  The caller
+ * owns host buffers; the library owns device memory.  A solver is used from
+ * one thread at a time (the reference's update takes &mut self,
+ * src/solver.rs:106); batches and servers synchronise internally.
+ *
+ * Reference citations are file:line within the bendy2d crate (src/...).
+ */
+#ifndef BENDY2D_H
+#define BENDY2D_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define B2D_OK 0
+#define B2D_ERR_NULL 1
+#define B2D_ERR_LINK_INDEX 2        /* a particle link breaks a < b < len; the reference panics in
+                                       ParticleLink::solve (src/link.rs:19-21) */
+#define B2D_ERR_CIRCLE_LINK_INDEX 3 /* same for circle links (src/link.rs:37-39) */
+#define B2D_ERR_POLY_LINK_INDEX 4   /* same inside Polygon::solve_links (src/polygon.rs:218-223) */
+#define B2D_ERR_ARG 5
+#define B2D_ERR_INDEX 6             /* getter index out of range: the reference returns None
+                                       (src/solver.rs:96-104) */
+#define B2D_ERR_CUDA 7
+#define B2D_ERR_DEVICE 8
+#define B2D_ERR_BUDGET 9            /* serving: request exceeds the device-memory budget */
+#define B2D_ERR_CAPACITY 10         /* caller buffer too small */
+#define B2D_ERR_STATE 11            /* call not valid in the object's current state */
+
+/* ---- modes and extension flags (not in the reference) ------------------ */
+#define B2D_MODE_REFERENCE 0 /* replays the reference's sequential link order exactly */
+#define B2D_MODE_FAST 1      /* links re-ordered by greedy colouring at build time */
+#define B2D_COLLIDE_PP 1u    /* particle-particle, hashed uniform grid */
+#define B2D_COLLIDE_PC 2u    /* particle-Circle */
+#define B2D_COLLIDE_PPOLY 4u /* particle-Polygon edge projection */
+
+/* ---- plain data, same fields as the reference -------------------------- */
+typedef struct { float x, y; } b2d_vec2;                    /* nalgebra Vector2<f32> */
+typedef struct { b2d_vec2 pos, prev_pos, acc; } b2d_particle; /* src/particle.rs:4-9 */
+typedef struct {                                           /* src/link.rs:4-10 */
+  uint64_t particle_a, particle_b; /* particle_a < particle_b (src/link.rs:6) */
+  float target_distance;
+  float stiffness; /* extension; 1.0 reproduces the reference */
+} b2d_link;
+typedef struct {                                           /* src/circle.rs:4-8 */
+  b2d_particle point;
+  float radius;
+  uint32_t is_static; /* extension: a static circle is not integrated */
+} b2d_circle;
+
+typedef struct b2d_solver b2d_solver;
+typedef struct b2d_batch b2d_batch;
+typedef struct b2d_server b2d_server;
+
+const char* b2d_last_error(void);
+const char* b2d_version(void);
+
+/* ---- Solver (src/solver.rs:19-189) ------------------------------------- */
+int b2d_solver_create(b2d_solver** out);                    /* Solver::new, src/solver.rs:34-50 */
+int b2d_solver_destroy(b2d_solver* s);
+int b2d_solver_clone(b2d_solver* s, b2d_solver** out);      /* #[derive(Clone)], src/solver.rs:19 */
+
+int b2d_set_gravity(b2d_solver* s, float x, float y);       /* pub gravity, src/solver.rs:21 */
+int b2d_get_gravity(b2d_solver* s, b2d_vec2* out);
+int b2d_set_bounds(b2d_solver* s, float px, float py, float sx, float sy); /* pub bounds, :22 */
+int b2d_get_bounds(b2d_solver* s, b2d_vec2* pos, b2d_vec2* size);
+int b2d_set_bounds_active(b2d_solver* s, int active);       /* pub bounds_active, :23 (never read) */
+int b2d_get_bounds_active(b2d_solver* s, int* out);
+
+int b2d_add_particle(b2d_solver* s, float x, float y);      /* Solver::add_particle, :52-54 */
+int b2d_add_circle(b2d_solver* s, const b2d_circle* c);     /* Solver::add_circle, :55-57 */
+int b2d_add_polygon(b2d_solver* s, size_t n_vertices, const b2d_particle* vertices,
+                    size_t n_links, const b2d_link* links, int is_static, b2d_vec2 center,
+                    float scale);                           /* Solver::add_polygon, :58-60 */
+int b2d_add_particle_link(b2d_solver* s, uint64_t a, uint64_t b, float target_distance);
+                                                            /* Solver::add_particle_link, :62-64 */
+int b2d_add_circle_link(b2d_solver* s, uint64_t a, uint64_t b, float target_distance);
+                                                            /* Solver::add_circle_link, :65-67 */
+
+/* extension: initial velocity (prev_pos) and bulk uploads; prev_xy may be NULL */
+int b2d_add_particle_prev(b2d_solver* s, float x, float y, float prev_x, float prev_y);
+int b2d_add_particles(b2d_solver* s, size_t n, const float* pos_xy, const float* prev_xy);
+int b2d_add_particle_links(b2d_solver* s, size_t n, const uint64_t* a, const uint64_t* b,
+                           const float* target_distance, const float* stiffness /* NULL = 1 */);
+
+/* Polygon::circle (src/polygon.rs:17-82) and Polygon::new (src/polygon.rs:84-123) added
+ * directly to the solver */
+int b2d_add_polygon_circle(b2d_solver* s, float radius, b2d_vec2 pos, size_t point_count,
+                           int is_static);
+int b2d_add_polygon_points(b2d_solver* s, size_t n, const b2d_vec2* points, int is_static);
+
+/* extension knobs (private or absent in the reference; defaults reproduce it) */
+int b2d_set_sub_steps(b2d_solver* s, uint32_t n);           /* private sub_steps = 1, :29,:47 */
+int b2d_get_sub_steps(b2d_solver* s, uint32_t* out);
+int b2d_set_link_iters(b2d_solver* s, uint32_t n);          /* apply_links repeated n times */
+int b2d_set_mode(b2d_solver* s, int mode);                  /* B2D_MODE_* */
+int b2d_set_collision(b2d_solver* s, uint32_t flags, float particle_radius, float grid_cell);
+int b2d_set_circle_static(b2d_solver* s, size_t index, int is_static);
+
+int b2d_update(b2d_solver* s, float dt);                    /* Solver::update, :106-116 */
+
+int b2d_get_particle_len(b2d_solver* s, size_t* out);       /* :69-71 */
+int b2d_get_circles_len(b2d_solver* s, size_t* out);        /* :72-74 */
+int b2d_get_polygons_len(b2d_solver* s, size_t* out);       /* :75-77 */
+int b2d_get_particle_links_len(b2d_solver* s, size_t* out);
+int b2d_get_circle_links_len(b2d_solver* s, size_t* out);
+int b2d_get_particle_links(b2d_solver* s, b2d_link* dst, size_t cap);   /* :79-81 */
+int b2d_get_circle_links(b2d_solver* s, b2d_link* dst, size_t cap);     /* :82-84 */
+int b2d_get_particles(b2d_solver* s, b2d_particle* dst, size_t cap);    /* :86-88 */
+int b2d_get_circles(b2d_solver* s, b2d_circle* dst, size_t cap);        /* :89-91 */
+int b2d_get_particle(b2d_solver* s, size_t index, b2d_particle* out);   /* :96-98 */
+int b2d_get_circle(b2d_solver* s, size_t index, b2d_circle* out);       /* :99-101 */
+/* get_polygons / get_polygon (:92-94, :102-104) */
+int b2d_get_polygon_info(b2d_solver* s, size_t index, size_t* n_vertices, size_t* n_links,
+                         int* is_static, b2d_vec2* center, float* scale);
+int b2d_get_polygon(b2d_solver* s, size_t index, b2d_particle* vertices, size_t cap_vertices,
+                    b2d_link* links, size_t cap_links);
+
+/* SoA state access (pos then prev, x/y interleaved, insertion order) */
+int b2d_read_state(b2d_solver* s, float* pos_xy, float* prev_xy);
+int b2d_write_state(b2d_solver* s, const float* pos_xy, const float* prev_xy);
+
+/* execution control */
+int b2d_set_stream(b2d_solver* s, void* cuda_stream);       /* NULL = library-owned stream */
+int b2d_synchronize(b2d_solver* s);
+int b2d_set_graphs(b2d_solver* s, int on);                  /* CUDA-graph replay (default on) */
+int b2d_set_profiling(b2d_solver* s, int on);               /* per-kernel CUDA-event timing */
+/* per-kernel times (ms) of the last profiled update: names joined by '\n' */
+int b2d_get_profile(b2d_solver* s, char* names, size_t names_cap, float* ms, size_t cap,
+                    size_t* count);
+int b2d_get_launch_count(b2d_solver* s, uint32_t* out);     /* kernel launches per update */
+
+/* end-to-end state transfer: the device state prefix of the solver (pos,
+ * prev, circles, polygons) from/to host memory (pinned for speed) */
+int b2d_state_bytes(b2d_solver* s, size_t* out);
+int b2d_state_upload_async(b2d_solver* s, const void* host_src);
+int b2d_state_download_async(b2d_solver* s, void* host_dst);
+
+/* planning introspection */
+typedef struct {
+  uint32_t bodies, group_bodies, serial_bodies, global_bodies;
+  uint64_t levels, ops;
+  uint32_t colours;
+  uint64_t device_bytes;
+} b2d_plan_stats;
+int b2d_get_plan_stats(b2d_solver* s, b2d_plan_stats* out);
+/* fast mode: the link order actually executed (world link ids) */
+int b2d_get_link_order(b2d_solver* s, uint64_t* order, size_t cap);
+
+/* ---- batch: many independent solvers stepped by one launch sequence ---- */
+int b2d_batch_create(b2d_batch** out);
+int b2d_batch_destroy(b2d_batch* b);       /* members return to their own engines */
+int b2d_batch_add(b2d_batch* b, b2d_solver* s);
+int b2d_batch_remove(b2d_batch* b, b2d_solver* s);
+int b2d_batch_update(b2d_batch* b, float dt);  /* Solver::update on every member */
+int b2d_batch_synchronize(b2d_batch* b);
+int b2d_batch_set_stream(b2d_batch* b, void* cuda_stream);
+int b2d_batch_set_profiling(b2d_batch* b, int on);
+int b2d_batch_get_profile(b2d_batch* b, char* names, size_t names_cap, float* ms, size_t cap,
+                          size_t* count);
+int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BENDY2D_H */

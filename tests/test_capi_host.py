@@ -1,0 +1,165 @@
+"""C ABI and host logic on the CPU: the library loads, exports every entry
+point include/bendy2d.h declares, plans worlds on the host, reports the
+reference's panic conditions as status codes, and refuses to run without a
+GPU (there is no CPU fallback)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "bendy2d.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(b2d_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    syms = declared_symbols()
+    assert len(syms) > 60
+    missing = [s for s in syms if not hasattr(native_lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(native_lib):
+    from bendy2d_gb300 import _native
+    bound = set(_native.SIGNATURES) | {"b2d_last_error", "b2d_version"}
+    assert set(declared_symbols()) <= bound
+
+
+def test_version(native_lib):
+    assert b"bendy2d" in native_lib.b2d_version()
+
+
+def test_solver_defaults_match_reference(native_lib):
+    """Solver::new, src/solver.rs:34-50."""
+    from bendy2d_gb300 import Solver
+    s = Solver()
+    assert s.gravity == pytest.approx((0.0, 98.2))
+    b = s.bounds
+    assert b.pos == (0.0, 0.0) and b.size == (100.0, 100.0)
+    assert s.bounds_active is True
+    assert s.sub_steps == 1
+    assert s.get_particle_len() == 0 and s.get_circles_len() == 0 and s.get_polygons_len() == 0
+
+
+def test_getters_return_none_out_of_range(native_lib):
+    """get_particle / get_circle / get_polygon return None (src/solver.rs:96-104)."""
+    from bendy2d_gb300 import Solver
+    s = Solver()
+    s.add_particle((1.0, 2.0))
+    assert s.get_particle(0).pos == (1.0, 2.0)
+    assert s.get_particle(1) is None
+    assert s.get_circle(0) is None
+    assert s.get_polygon(0) is None
+
+
+def test_polygon_builders_match_oracle(native_lib):
+    """Polygon::circle / Polygon::new built by the product's host code equal
+    the oracle's restatement bit for bit."""
+    from oracle import Oracle
+    from bendy2d_gb300 import Polygon
+    from helpers import same_bits
+    for n in (3, 5, 8, 13):
+        g = Polygon.circle(7.5, (40.0, 60.0), n, False)
+        o = Oracle()
+        o.add_polygon_circle(7.5, 40.0, 60.0, n, False)
+        pos, _, ctr = o.polygons()[0]
+        assert same_bits(np.asarray([p.pos for p in g.particles]), pos)
+        assert same_bits(np.asarray(g.center), ctr)
+        a, b, t = o.polygon_links(0)
+        assert [l.link.particle_a for l in g.particle_links] == a.tolist()
+        assert [l.link.particle_b for l in g.particle_links] == b.tolist()
+        assert same_bits([l.link.target_distance for l in g.particle_links], t)
+    pts = [(1.0, 1.0), (5.0, 1.5), (6.0, 7.0), (0.5, 4.0)]
+    g = Polygon.new(pts, True)
+    o = Oracle()
+    o.add_polygon_points(np.asarray(pts, np.float32), True)
+    pos, _, ctr = o.polygons()[0]
+    assert same_bits(np.asarray([p.pos for p in g.particles]), pos)
+    assert same_bits(np.asarray(g.center), ctr)
+    assert g.is_static
+
+
+@pytest.mark.parametrize("bad,code", [((1, 0), 2), ((0, 0), 2), ((0, 2), 2)])
+def test_bad_particle_links_are_status_codes(native_lib, bad, code):
+    """The reference panics in ParticleLink::solve (src/link.rs:19-21)."""
+    from bendy2d_gb300 import B2DError, Link, Solver
+    s = Solver()
+    s.add_particle((1.0, 1.0))
+    s.add_particle((2.0, 2.0))
+    s.add_particle_link(Link(bad[0], bad[1], 1.0))
+    with pytest.raises(B2DError) as e:
+        s.plan_stats()
+    assert e.value.code == code
+
+
+def test_bad_polygon_circle_is_status_code(native_lib):
+    from bendy2d_gb300 import B2DError, Solver
+    s = Solver()
+    s.add_polygon_circle(5.0, (50.0, 50.0), 2, False)
+    with pytest.raises(B2DError) as e:
+        s.plan_stats()
+    assert e.value.code == 4
+
+
+def test_update_without_gpu_fails_loudly(native_lib):
+    from conftest import HAS_GPU
+    if HAS_GPU:
+        pytest.skip("a GPU is present")
+    from bendy2d_gb300 import B2DError, Solver
+    s = Solver()
+    s.add_particle((1.0, 1.0))
+    with pytest.raises(B2DError) as e:
+        s.update(0.016)
+    assert e.value.code == 7 and "no CPU path" in str(e.value)
+
+
+def test_plan_cloth_grid(native_lib):
+    """One 32x32 cloth: one group body whose full-step schedule merges all
+    8 sub-steps x 4 link passes (+ integrate) into 413 levels."""
+    from bendy2d_gb300 import scenes
+    s = scenes.config1(steps=1).to_solver()
+    st = s.plan_stats()
+    assert st["bodies"] == 1 and st["group_bodies"] == 1 and st["serial_bodies"] == 0
+    assert st["ops"] == 8 * (4 * 3906 + 1024)
+    assert st["levels"] == 413
+
+
+def test_plan_rings_run_serially(native_lib):
+    """Rings with a hub are chains in the reference's order (every spoke shares
+    the centre), so they go to the serial executor."""
+    from bendy2d_gb300 import scenes
+    rng = np.random.default_rng(3)
+    sc = scenes.config3_world(rng, 900)
+    st = sc.to_solver().plan_stats()
+    assert st["serial_bodies"] >= 1 and st["group_bodies"] == 0
+
+
+def test_fast_mode_colouring_is_proper(native_lib):
+    """Fast mode: no two links of one colour class share a particle, and the
+    order is a permutation of the links."""
+    from bendy2d_gb300 import MODE_FAST, scenes
+    sc = scenes.config1(steps=1)
+    sc.mode = MODE_FAST
+    s = sc.to_solver()
+    order = s.link_order()
+    assert sorted(order.tolist()) == list(range(len(sc.la)))
+    st = s.plan_stats()
+    assert 4 <= st["colours"] <= 16
+    # replay the greedy colouring: consecutive runs with disjoint particles
+    la, lb = sc.la[order.astype(np.int64)], sc.lb[order.astype(np.int64)]
+    seen, classes = set(), 0
+    for a, b in zip(la.tolist(), lb.tolist()):
+        if a in seen or b in seen:
+            seen = set()
+            classes += 1
+        seen.update((a, b))
+    assert classes + 1 <= st["colours"]
+    # fast mode needs far fewer levels than reference order
+    ref = scenes.config1(steps=1).to_solver().plan_stats()
+    assert st["levels"] < ref["levels"]
