@@ -12,6 +12,7 @@
 // run ahead into later passes (the critical path of a 32x32 cloth step drops
 // from 4032 to ~413 levels).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -78,10 +79,74 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   uint32_t* dst = ops.data() + d.op0;
   std::vector<uint32_t> fill(start.begin(), start.end());
   for (size_t i = 0; i < total; ++i) dst[fill[lvl_of[i]]++] = op_of[i];
+  // self-check: every op names a link or particle of the body, and the level
+  // offsets cover the op list exactly
+  for (size_t i = 0; i < total; ++i) {
+    const uint32_t op = dst[i];
+    if ((op & OP_INTEG) ? (op & ~OP_INTEG) >= np : op >= nl) std::abort();
+  }
+  if (lvl.back() != total) std::abort();
   const uint32_t id = (uint32_t)scheds.size();
   scheds.push_back(d);
   index.emplace(std::move(key), id);
   return id;
+}
+
+// Bounds check of a finished image: every index a kernel dereferences must
+// land inside the world's arrays.  Runs on every plan (linear in the size of
+// the world); a failure is a planner bug and stops the world from reaching
+// the GPU.
+static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::string* why) {
+  auto bad = [&](const std::string& m) {
+    if (why) *why = "internal planner check failed: " + m;
+    return false;
+  };
+  const DWorld& P = im.params;
+  if (im.pos.size() != P.np || im.prev.size() != P.np) return bad("particle arrays");
+  if (im.bodies.size() != P.nb) return bad("body count");
+  for (const DBody& B : im.bodies) {
+    if ((size_t)B.i0 + B.np > im.bidx.size()) return bad("body particle range");
+    if ((size_t)B.l0 + B.nl > im.lab.size() || im.lab.size() != im.lrest.size() ||
+        im.lab.size() != im.lstiff.size())
+      return bad("body link range");
+    for (uint32_t i = 0; i < B.np; ++i)
+      if (im.bidx[B.i0 + i] >= P.np) return bad("body particle index");
+    const uint32_t lim = B.local ? B.np : P.np;
+    if (B.local && B.np > 65535u) return bad("local body too large");
+    for (uint32_t k = 0; k < B.nl; ++k) {
+      const uint2 e = im.lab[B.l0 + k];
+      if (e.x >= lim || e.y >= lim || e.x == e.y) return bad("link endpoint");
+    }
+  }
+  for (const GroupBody& g : im.groups) {
+    if (g.body >= im.bodies.size()) return bad("group body id");
+    const DBody& B = im.bodies[g.body];
+    if (B.sched >= reg.scheds.size()) return bad("schedule id");
+    const DSched& S = reg.scheds[B.sched];
+    if ((size_t)S.op0 + S.nops > reg.ops.size() || (size_t)S.lvl0 + S.nlvl + 1 > reg.lvl.size())
+      return bad("schedule range");
+    if (g.smem && !B.local) return bad("shared-memory body without local links");
+    if (g.T < 32 || g.T % 32) return bad("group size");
+  }
+  for (uint32_t b : im.serials)
+    if (b >= im.bodies.size() || im.bodies[b].local) return bad("serial body");
+  if (im.cpos.size() != P.nc || im.crad.size() != P.nc) return bad("circle arrays");
+  for (const uint2& e : im.clab)
+    if (e.x >= P.nc || e.y >= P.nc) return bad("circle link");
+  if (im.polys.size() != P.ng || im.pcenter.size() != P.ng) return bad("polygon arrays");
+  for (const DPoly& g : im.polys) {
+    if ((size_t)g.v0 + g.nv > im.vpos.size()) return bad("polygon vertex range");
+    if ((size_t)g.l0 + g.nl > im.plab.size()) return bad("polygon link range");
+    for (uint32_t k = 0; k < g.nl; ++k) {
+      const uint2 e = im.plab[g.l0 + k];
+      if (e.x >= g.nv || e.y >= g.nv) return bad("polygon link endpoint");
+    }
+  }
+  const size_t nst = P.ng >= 2 ? (size_t)P.ng * (P.ng - 1) + 1 : 0;
+  if (im.stage_off.size() != nst) return bad("polygon stage table");
+  for (size_t i = 1; i < nst; ++i)
+    if (im.stage_off[i] < im.stage_off[i - 1]) return bad("polygon stage order");
+  return true;
 }
 
 namespace {
@@ -326,6 +391,7 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
       }
     im.stage_off.push_back(acc);
   }
+  if (!check_image(im, reg, why)) return ERR_STATE;
   return OK;
 }
 

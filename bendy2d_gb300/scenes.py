@@ -190,8 +190,10 @@ def config2(seed: int = 0, n_bodies: int = 64, box: float = 2000.0, n_circles: i
     h = (1.0 / 60.0) / 8.0
     circles = [_circle(rng.uniform(0.0, box, 2), rng.uniform(5.0, 30.0), False)
                for _ in range(n_circles)]
-    polys = [{"points": convex_polygon(rng, rng.uniform(50.0, box - 50.0, 2),
-                                       rng.uniform(10.0, 50.0), int(rng.integers(4, 9))),
+    m = min(50.0, 0.25 * box)  # small test boxes shrink the hull radius range
+    polys = [{"points": convex_polygon(rng, rng.uniform(m, box - m, 2),
+                                       rng.uniform(min(10.0, 0.5 * m), m),
+                                       int(rng.integers(4, 9))),
               "static": False} for _ in range(n_polys)]
     sc = _assemble("config2_64grids", bodies, circles=circles, polygons=polys,
                    bounds=(0.0, 0.0, box, box), sub_steps=8, link_iters=4, collide=collide,
