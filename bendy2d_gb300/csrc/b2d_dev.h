@@ -37,9 +37,18 @@ struct DPoly {
   uint32_t is_static, pad;
 };
 
+// A level schedule is stored as a stream of self-describing chunks of at most
+// SCHED_CHUNK_WORDS 32-bit words, each 16-byte aligned so that one bulk copy
+// (TMA, cp.async.bulk) moves it into shared memory:
+//   word 0            nseg
+//   words 1..nseg     end offset of each segment within the op list
+//   words 1+nseg..    ops of the chunk (link index, or OP_INTEG | particle)
+// A segment is a whole level or a piece of one; a group barrier follows
+// every segment.
+constexpr uint32_t SCHED_CHUNK_WORDS = 4096;
 struct DSched {
-  uint32_t lvl0, nlvl;   // level offsets at lvl[lvl0 .. lvl0+nlvl]
-  uint32_t op0, nops;    // ops at ops[op0 .. op0+nops)
+  uint32_t chunk0, nchunks;  // chunk_off / chunk_len entries
+  uint32_t nlvl, nops;
 };
 
 struct DWorld {
@@ -52,7 +61,8 @@ struct DWorld {
   uint32_t flags;        // COLLIDE_* bits
   uint32_t slot;         // stable id (hash salt for the shared grid)
   uint32_t np, nb, nc, ncl, ng;
-  uint32_t pad;
+  uint32_t gb0, gmask;   // extension grid: this world's buckets [gb0, gb0 + gmask]
+  uint32_t gp0, pad;     // extension grid: this world's particle scratch offset
   // solver particles
   float2* pos[2];        // ping-pong positions; pos[0] holds the state between steps
   float2* prev;
@@ -75,24 +85,28 @@ struct DWorld {
   uint32_t* stage_off;   // polygon-pair test offsets, see rigid_phase_a
 };
 
-// Shared (engine-wide) read-only schedule registry.
+// Shared (engine-wide) read-only schedule registry, plus the device error
+// word that bounded waits set instead of trapping.
 struct DScheds {
   const DSched* scheds;
-  const uint32_t* lvl;
-  const uint32_t* ops;
+  const uint32_t* chunk_off;  // word offset of each chunk in `stream`
+  const uint32_t* chunk_len;  // words (multiple of 4)
+  const uint32_t* stream;
+  uint32_t* err;
 };
+enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u };
 
-// Extension broadphase: hashed uniform grid with K slots per bucket and an
-// overflow list sized so that nothing is ever dropped.
-constexpr uint32_t BUCKET_K = 8;
+// Extension broadphase: hashed uniform grid built by a counting sort each
+// sub-step.  Every world with particle collisions owns a power-of-two range
+// of buckets; a bucket's entries are contiguous in `sorted`.
+constexpr uint32_t SCAN_TILE = 4096;  // buckets per scan block (1024 threads x 4)
 struct DGrid {
-  uint32_t* count;       // nbuckets
-  uint4* slots;          // nbuckets * BUCKET_K : {world, particle, cx, cy}
-  uint4* overflow;       // cap entries
-  uint32_t* ovf_bucket;  // cap entries
-  uint32_t* ovf_n;       // [0] = used
-  uint32_t ovf_cap;
-  uint32_t mask;         // nbuckets - 1
+  uint32_t* count;       // nbuckets: entries per bucket
+  uint32_t* start;       // nbuckets: exclusive prefix sum of count
+  uint32_t* partial;     // per scan tile: sum of its counts
+  uint2* pbr;            // per particle: (bucket, rank within bucket)
+  uint4* sorted;         // per particle: {pos.x bits, pos.y bits, particle, cell x}
+  uint32_t nbuckets;
 };
 
 }  // namespace b2d

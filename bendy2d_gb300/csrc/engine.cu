@@ -38,6 +38,8 @@ static uint32_t pow2ceil_u(uint32_t x) {
 }
 
 static int g_smem_optin = -1;
+static int g_num_sms = 0;
+static constexpr uint64_t kRigidSmemCap = 96 * 1024;
 
 Engine::Engine(cudaStream_t stream) : stream_(stream) {
   if (!stream_) {
@@ -49,10 +51,16 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g_smem_optin = v;
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    for (auto fn : {k_rigid<0>, k_rigid<1>, k_rigid<2>, k_rigid<3>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRigidSmemCap);
     cudaFuncSetAttribute(k_exec_groups<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
     cudaFuncSetAttribute(k_exec_groups<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    cudaFuncSetAttribute(k_exec_groups<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    cudaFuncSetAttribute(k_exec_groups<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   }
-  tune_.smem_max = std::min<uint32_t>(tune_.smem_max, (uint32_t)std::max(g_smem_optin, 48 * 1024));
+  tune_.smem_max = std::min<uint32_t>(
+      tune_.smem_max, (uint32_t)std::max(g_smem_optin - (int)STREAM_BYTES, 16 * 1024));
 }
 
 Engine::~Engine() {
@@ -62,8 +70,10 @@ Engine::~Engine() {
     if (s.block) cudaFree(s.block);
   cudaFree(d_worlds_);
   cudaFree(d_scheds_);
-  cudaFree(d_lvl_);
-  cudaFree(d_ops_);
+  cudaFree(d_chunk_off_);
+  cudaFree(d_chunk_len_);
+  cudaFree(d_stream_);
+  cudaFree(d_err_);
   cudaFree(d_lists_);
   cudaFree(d_wlists_);
   cudaFree(d_grid_);
@@ -224,25 +234,47 @@ int Engine::set_params(uint32_t slot) {
 }
 
 int Engine::upload_registry() {
-  auto grow = [&](auto*& ptr, size_t& cap, size_t need, size_t elem) -> int {
+  if (!d_err_) {
+    B2D_CUDA(cudaMalloc(&d_err_, 16));
+    B2D_CUDA(cudaMemsetAsync(d_err_, 0, 16, stream_));
+    invalidate_graph();
+  }
+  auto grow = [&](uint32_t*& ptr, size_t& cap, size_t need, size_t elem) -> int {
     if (need <= cap) return OK;
     size_t nc = std::max(need, cap * 2 + 1024);
     void* d = nullptr;
     B2D_CUDA(cudaMalloc(&d, nc * elem));
     B2D_CUDA(cudaStreamSynchronize(stream_));
     cudaFree(ptr);
-    ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(d);
+    ptr = static_cast<uint32_t*>(d);
     cap = nc;
     invalidate_graph();
     return OK;
   };
-  const bool grew = reg_.scheds.size() > scheds_cap_ || reg_.lvl.size() > lvl_cap_ ||
-                    reg_.ops.size() > ops_cap_;
+  bool grew = false;
   int st;
-  if ((st = grow(d_scheds_, scheds_cap_, reg_.scheds.size(), sizeof(DSched))) != OK) return st;
-  if ((st = grow(d_lvl_, lvl_cap_, reg_.lvl.size(), 4)) != OK) return st;
-  if ((st = grow(d_ops_, ops_cap_, reg_.ops.size(), 4)) != OK) return st;
-  if (grew) reg_.uploaded_scheds = reg_.uploaded_lvl = reg_.uploaded_ops = 0;
+  if (reg_.scheds.size() > scheds_cap_) {
+    size_t nc = std::max(reg_.scheds.size(), scheds_cap_ * 2 + 64);
+    DSched* d = nullptr;
+    B2D_CUDA(cudaMalloc(&d, nc * sizeof(DSched)));
+    B2D_CUDA(cudaStreamSynchronize(stream_));
+    cudaFree(d_scheds_);
+    d_scheds_ = d;
+    scheds_cap_ = nc;
+    grew = true;
+    invalidate_graph();
+  }
+  if (reg_.chunk_off.size() > chunks_cap_) {
+    size_t cap2 = chunks_cap_;
+    if ((st = grow(d_chunk_off_, chunks_cap_, reg_.chunk_off.size(), 4)) != OK) return st;
+    if ((st = grow(d_chunk_len_, cap2, reg_.chunk_len.size(), 4)) != OK) return st;
+    grew = true;
+  }
+  if (reg_.stream.size() > stream_cap_) {
+    if ((st = grow(d_stream_, stream_cap_, reg_.stream.size(), 4)) != OK) return st;
+    grew = true;
+  }
+  if (grew) reg_.uploaded_scheds = reg_.uploaded_chunks = reg_.uploaded_stream = 0;
   auto put = [&](void* dst, const void* src, size_t from, size_t to, size_t elem) -> int {
     if (to > from)
       B2D_CUDA(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + from * elem,
@@ -251,36 +283,56 @@ int Engine::upload_registry() {
     return OK;
   };
   if ((st = put(d_scheds_, reg_.scheds.data(), reg_.uploaded_scheds, reg_.scheds.size(), sizeof(DSched))) != OK) return st;
-  if ((st = put(d_lvl_, reg_.lvl.data(), reg_.uploaded_lvl, reg_.lvl.size(), 4)) != OK) return st;
-  if ((st = put(d_ops_, reg_.ops.data(), reg_.uploaded_ops, reg_.ops.size(), 4)) != OK) return st;
+  if ((st = put(d_chunk_off_, reg_.chunk_off.data(), reg_.uploaded_chunks, reg_.chunk_off.size(), 4)) != OK) return st;
+  if ((st = put(d_chunk_len_, reg_.chunk_len.data(), reg_.uploaded_chunks, reg_.chunk_len.size(), 4)) != OK) return st;
+  if ((st = put(d_stream_, reg_.stream.data(), reg_.uploaded_stream, reg_.stream.size(), 4)) != OK) return st;
+  const bool any = reg_.uploaded_scheds != reg_.scheds.size() ||
+                   reg_.uploaded_stream != reg_.stream.size();
   reg_.uploaded_scheds = reg_.scheds.size();
-  reg_.uploaded_lvl = reg_.lvl.size();
-  reg_.uploaded_ops = reg_.ops.size();
-  B2D_CUDA(cudaStreamSynchronize(stream_));
+  reg_.uploaded_chunks = reg_.chunk_off.size();
+  reg_.uploaded_stream = reg_.stream.size();
+  if (any) B2D_CUDA(cudaStreamSynchronize(stream_));
   return OK;
 }
 
-int Engine::ensure_grid(size_t np_ext) {
-  if (np_ext <= grid_np_ && d_grid_) return OK;
-  size_t nb = pow2ceil_u((uint32_t)std::max<size_t>(np_ext, 1024));
-  size_t cap = std::max<size_t>(np_ext, 1);
+int Engine::check_device_error() {
+  if (!d_err_) return OK;
+  uint32_t e = 0;
+  B2D_CUDA(cudaMemcpyAsync(&e, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
+  B2D_CUDA(cudaStreamSynchronize(stream_));
+  if (e) {
+    B2D_CUDA(cudaMemsetAsync(d_err_, 0, 4, stream_));
+    last_error = "device error word " + std::to_string(e) +
+                 ((e & ERR_BIT_TMA_TIMEOUT) ? " (a bulk-copy wait timed out)" : "");
+    return ERR_DEVICE;
+  }
+  return OK;
+}
+
+int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
+  if (nbuckets <= grid_.nbuckets && np_pp <= grid_np_ && d_grid_) return OK;
+  const size_t nb = std::max(nbuckets, (size_t)grid_.nbuckets);
+  const size_t np = std::max<size_t>(std::max(np_pp, grid_np_), 1);
+  const size_t ntiles = (nb + SCAN_TILE - 1) / SCAN_TILE;
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
-  size_t o_count = seg(nb * 4), o_slots = seg(nb * BUCKET_K * 16), o_ovf = seg(cap * 16),
-         o_ovfb = seg(cap * 4), o_ovfn = seg(16);
+  const size_t o_count = seg(nb * 4), o_start = seg(nb * 4), o_part = seg(ntiles * 4),
+               o_pbr = seg(np * 8), o_sorted = seg(np * 16);
   B2D_CUDA(cudaStreamSynchronize(stream_));
+  if (d_grid_) dev_bytes_ -= grid_bytes_;
   cudaFree(d_grid_);
   d_grid_ = nullptr;
   B2D_CUDA(cudaMalloc(&d_grid_, bytes));
   B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
   grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
-  grid_.slots = reinterpret_cast<uint4*>(d_grid_ + o_slots);
-  grid_.overflow = reinterpret_cast<uint4*>(d_grid_ + o_ovf);
-  grid_.ovf_bucket = reinterpret_cast<uint32_t*>(d_grid_ + o_ovfb);
-  grid_.ovf_n = reinterpret_cast<uint32_t*>(d_grid_ + o_ovfn);
-  grid_.ovf_cap = (uint32_t)cap;
-  grid_.mask = (uint32_t)(nb - 1);
-  grid_np_ = np_ext;
+  grid_.start = reinterpret_cast<uint32_t*>(d_grid_ + o_start);
+  grid_.partial = reinterpret_cast<uint32_t*>(d_grid_ + o_part);
+  grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o_pbr);
+  grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o_sorted);
+  grid_.nbuckets = (uint32_t)nb;
+  grid_np_ = np;
+  grid_bytes_ = bytes;
+  dev_bytes_ += bytes;
   invalidate_graph();
   return OK;
 }
@@ -295,6 +347,8 @@ int Engine::rebuild_lists() {
   smax_ext_ = 0;
   any_pp_ = false;
   size_t np_ext = 0;
+  size_t nbuckets = 0, np_pp = 0;
+  uint64_t rigid_smem = 0;
   std::map<std::tuple<uint32_t, bool, bool, uint32_t>, size_t> cls;
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
@@ -302,7 +356,7 @@ int Engine::rebuild_lists() {
     const WorldImage& im = s.img;
     const bool full = !im.ext;
     for (const GroupBody& gb : im.groups) {
-      const uint32_t rc = gb.smem ? std::max<uint32_t>(pow2ceil_u(gb.region), 1024) : 0u;
+      const uint32_t rc = gb.smem ? (gb.region + 4095u) & ~4095u : 0u;
       auto key = std::make_tuple(gb.T, gb.smem, full, rc);
       auto it = cls.find(key);
       if (it == cls.end()) {
@@ -314,7 +368,7 @@ int Engine::rebuild_lists() {
         if (gb.smem && c.region < gb.region) c.region = gb.region;
         uint32_t G = gb.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / gb.T);
         if (gb.T != 32) G = std::min<uint32_t>(G, 15);
-        if (c.smem) G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / c.region));
+        G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / (c.region + STREAM_BYTES)));
         c.G = G;
         it = cls.emplace(key, classes_.size()).first;
         classes_.push_back(std::move(c));
@@ -323,12 +377,33 @@ int Engine::rebuild_lists() {
     }
     for (uint32_t b : im.serials) (full ? serial_full_ : serial_links_).push_back(make_uint2(si, b));
     const bool rigid = im.params.nc > 0 || im.params.ng > 0;
+    if (rigid) {
+      const uint64_t ng = im.polys.size(), nc = im.cpos.size(), nv = im.vpos.size();
+      // same expression as rigid_smem_bytes() in kernels.cuh
+      const uint64_t need = 48 * ng + 28 * nc + 12 * im.clab.size() + 24 * nv +
+                            12 * im.plab.size() + 4 * im.stage_off.size() + 256;
+      if (need <= kRigidSmemCap) rigid_smem = std::max<uint64_t>(rigid_smem, need);
+    }
     if (full) {
       if (rigid) rigid_full_.push_back(si);
     } else {
       if (rigid) rigid_ext_.push_back(si);
       smax_ext_ = std::max(smax_ext_, im.params.S);
-      if (im.params.flags & COLLIDE_PP) any_pp_ = true;
+      if (im.params.flags & COLLIDE_PP) {
+        any_pp_ = true;
+        // this world's bucket range: a power of two >= 2 x its particles
+        const uint32_t nbw = pow2ceil_u(std::max<uint32_t>(2u * im.params.np, 64u));
+        if (h_worlds_[si].gb0 != (uint32_t)nbuckets || h_worlds_[si].gmask != nbw - 1 ||
+            h_worlds_[si].gp0 != (uint32_t)np_pp) {
+          h_worlds_[si].gb0 = (uint32_t)nbuckets;
+          h_worlds_[si].gmask = nbw - 1;
+          h_worlds_[si].gp0 = (uint32_t)np_pp;
+          B2D_CUDA(cudaMemcpyAsync(d_worlds_ + si, &h_worlds_[si], sizeof(DWorld),
+                                   cudaMemcpyHostToDevice, stream_));
+        }
+        nbuckets += nbw;
+        np_pp += im.params.np;
+      }
       for (uint32_t st = 0; st < im.params.np; st += CHUNK) chunks_.push_back(make_uint2(si, st));
       np_ext += im.params.np;
     }
@@ -374,10 +449,13 @@ int Engine::rebuild_lists() {
   if (!wl.empty())
     B2D_CUDA(cudaMemcpyAsync(d_wlists_, wl.data(), wl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
   B2D_CUDA(cudaStreamSynchronize(stream_));
-  if (np_ext > 0) {
-    int st = ensure_grid(np_ext);
+  (void)np_ext;
+  if (nbuckets > 0) {
+    int st = ensure_grid(nbuckets, np_pp);
     if (st != OK) return st;
   }
+  grid_used_ = (uint32_t)nbuckets;
+  rigid_smem_ = (uint32_t)rigid_smem;
   lists_dirty_ = false;
   invalidate_graph();
   return OK;
@@ -406,22 +484,22 @@ int Engine::launch_all(bool profiling) {
       if (!found) prof_.emplace_back(name, ms);
     }
   };
-  const DScheds SC{d_scheds_, d_lvl_, d_ops_};
+  const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_};
   const DWorld* W = d_worlds_;
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
       if (c.full != full || c.items.empty()) continue;
       const uint32_t n = (uint32_t)c.items.size();
       const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
-      const size_t sm = c.smem ? (size_t)c.G * c.region : 0;
+      const size_t sm = (size_t)c.G * (c.region + STREAM_BYTES);
       const uint2* L = d_lists_ + c.dev_off;
       const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
                               : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
       timed(name, [&] {
         if (full && c.smem) k_exec_groups<true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
-        else if (full) k_exec_groups<true, false><<<grid, block, 0, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
+        else if (full) k_exec_groups<true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
         else if (c.smem) k_exec_groups<false, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
-        else k_exec_groups<false, false><<<grid, block, 0, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
+        else k_exec_groups<false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
       });
     }
   };
@@ -435,7 +513,7 @@ int Engine::launch_all(bool profiling) {
   }
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
-    timed("rigid_full", [&] { k_rigid<0><<<n, 128, 0, stream_>>>(W, d_wlists_, n, 0); });
+    timed("rigid_full", [&] { k_rigid<0><<<n, 128, rigid_smem_, stream_>>>(W, d_wlists_, n, 0, rigid_smem_); });
   }
   // worlds with extension collisions: per sub-step pipeline
   const uint32_t nch = (uint32_t)chunks_.size();
@@ -453,17 +531,25 @@ int Engine::launch_all(bool profiling) {
     }
     if (nre) {
       timed("rigid_ext", [&] {
-        if (s == 0) k_rigid<1><<<nre, 128, 0, stream_>>>(W, RE, nre, s);
-        else k_rigid<3><<<nre, 128, 0, stream_>>>(W, RE, nre, s);
+        if (s == 0) k_rigid<1><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, s, rigid_smem_);
+        else k_rigid<3><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, s, rigid_smem_);
       });
     }
     if (any_pp_) {
+      const uint32_t nt = (grid_used_ + SCAN_TILE - 1) / SCAN_TILE;
       timed("grid_clear", [&] {
-        cudaMemsetAsync(grid_.count, 0, ((size_t)grid_.mask + 1) * 4, stream_);
-        cudaMemsetAsync(grid_.ovf_n, 0, 8, stream_);
+        cudaMemsetAsync(grid_.count, 0, (size_t)grid_used_ * 4, stream_);
       }, false);
-      timed("grid_insert", [&] {
-        k_grid_insert<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      timed("grid_count", [&] {
+        k_grid_count<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      });
+      timed("grid_scan", [&] {
+        k_scan_reduce<<<nt, 1024, 0, stream_>>>(grid_, grid_used_);
+        k_scan_apply<<<nt, 1024, 0, stream_>>>(grid_, grid_used_);
+      });
+      ++launches_;
+      timed("grid_scatter", [&] {
+        k_grid_scatter<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });
     }
     timed("collide_integrate", [&] {
@@ -471,7 +557,7 @@ int Engine::launch_all(bool profiling) {
     });
   }
   if (smax_ext_ > 0) {
-    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, 0, stream_>>>(W, RE, nre, smax_ext_ - 1); });
+    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
     timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
   }
   if (profiling) {
@@ -516,7 +602,7 @@ int Engine::step() {
 
 int Engine::sync() {
   B2D_CUDA(cudaStreamSynchronize(stream_));
-  return OK;
+  return check_device_error();
 }
 
 int Engine::state_span(uint32_t slot, void** dptr, size_t* bytes) {
@@ -533,6 +619,8 @@ int Engine::download(uint32_t slot) {
   if (!buf.empty())
     B2D_CUDA(cudaMemcpyAsync(buf.data(), s.block, s.L.state_bytes, cudaMemcpyDeviceToHost, stream_));
   B2D_CUDA(cudaStreamSynchronize(stream_));
+  int est = check_device_error();
+  if (est != OK) return est;
   WorldHost& w = *s.host;
   const float2* p = buf.data();
   const size_t np = s.img.pos.size();

@@ -32,9 +32,8 @@ struct PlanTuning {
 struct SchedRegistry {
   std::unordered_map<std::string, uint32_t> index;
   std::vector<DSched> scheds;
-  std::vector<uint32_t> lvl;
-  std::vector<uint32_t> ops;
-  size_t uploaded_scheds = 0, uploaded_lvl = 0, uploaded_ops = 0;
+  std::vector<uint32_t> chunk_off, chunk_len, stream;
+  size_t uploaded_scheds = 0, uploaded_chunks = 0, uploaded_stream = 0;
   uint32_t get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I, bool full);
 };
 
@@ -138,7 +137,7 @@ class Engine {
   int rebuild_lists();
   int upload_registry();
   int ensure_table(size_t n);
-  int ensure_grid(size_t np_ext);
+  int ensure_grid(size_t nbuckets, size_t np_ext);
   int launch_all(bool profiling);
   void invalidate_graph();
   int fill_world_record(uint32_t slot);
@@ -155,10 +154,13 @@ class Engine {
   std::vector<DWorld> h_worlds_;
   DSched* d_scheds_ = nullptr;
   size_t scheds_cap_ = 0;
-  uint32_t* d_lvl_ = nullptr;
-  size_t lvl_cap_ = 0;
-  uint32_t* d_ops_ = nullptr;
-  size_t ops_cap_ = 0;
+  uint32_t* d_chunk_off_ = nullptr;
+  uint32_t* d_chunk_len_ = nullptr;
+  size_t chunks_cap_ = 0;
+  uint32_t* d_stream_ = nullptr;
+  size_t stream_cap_ = 0;
+  uint32_t* d_err_ = nullptr;  // device error word (bounded waits)
+  int check_device_error();
   // work lists
   std::vector<LaunchClass> classes_;
   std::vector<uint2> serial_full_, serial_links_, chunks_;
@@ -171,6 +173,9 @@ class Engine {
   size_t off_rigid_ext_ = 0;
   uint32_t smax_ext_ = 0;
   bool any_pp_ = false;
+  uint32_t rigid_smem_ = 0;
+  uint32_t grid_used_ = 0;
+  size_t grid_bytes_ = 0;
   bool lists_dirty_ = true;
   // broadphase
   DGrid grid_{};

@@ -13,7 +13,6 @@
 
 namespace b2d {
 
-#define B2D_NONE 0xFFFFFFFFu
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -82,6 +81,61 @@ __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
 }
 
 // ----------------------------------------------------------------------------
+// Bulk-copy (TMA) helpers.  One elected thread issues cp.async.bulk into
+// shared memory and completion is tracked by an mbarrier transaction count.
+// Every wait is bounded (about two seconds of SM clock); on timeout the
+// kernel records ERR_BIT_TMA_TIMEOUT in the device error word and returns
+// instead of trapping.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// bytes must be a multiple of 16; src and dst 16-byte aligned
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > WAIT_LIMIT_CYCLES) return false;
+  }
+  return true;
+}
+
+// shared bytes per group beyond the body region: two chunk buffers, two
+// mbarriers and a broadcast word
+constexpr uint32_t STREAM_BYTES = 2 * SCHED_CHUNK_WORDS * 4 + 32;
+
+// ----------------------------------------------------------------------------
 // Body executor (block / warp granularity).
 //
 // Each CTA holds G groups of T threads; group g runs work item
@@ -93,16 +147,16 @@ __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
 // integrate, src/solver.rs:109-115); LINKS-only schedules cover the I link
 // passes of one sub-step (extension pipeline).
 //
-// SMEM: the body's positions (and prev) and links live in shared memory; the
-// op stream is read from global memory with a two-level register prefetch so
-// its latency stays off the per-level critical path.  !SMEM runs the same
-// schedule directly on global memory (bodies too large for shared memory).
+// The schedule streams into shared memory in chunks by double-buffered bulk
+// copies, so a level costs shared-memory latency only.  SMEM keeps the body's
+// positions (and prev) and links in shared memory too; !SMEM runs the same
+// schedule on global memory (bodies too large for one CTA).
 // ----------------------------------------------------------------------------
 template <bool FULL, bool SMEM>
 __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
                               uint32_t G, uint32_t region_bytes, uint32_t cur, uint32_t sub) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
   const uint32_t item = blockIdx.x * G + g;
   if (item >= nlist) return;  // the whole group leaves; its barrier is private
@@ -110,6 +164,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   const DWorld& W = worlds[wi.x];
   if (!FULL && sub >= W.S) return;  // world already finished its sub-steps
   const DBody B = W.bodies[wi.y];
+  const DSched S = SC.scheds[B.sched];
   const uint32_t* bidx = W.bidx + B.i0;
   float2* gp = W.pos[cur];
   float2* gq = W.prev;
@@ -120,13 +175,24 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   DWorld Wb;  // bounds only
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
 
+  unsigned char* base = smem + (size_t)g * (region_bytes + STREAM_BYTES);
+  uint32_t* cbuf = reinterpret_cast<uint32_t*>(base + region_bytes);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(cbuf + 2 * SCHED_CHUNK_WORDS);
+  volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(bar + 2);
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    if (S.nchunks > 0)
+      bulk_load(cbuf, SC.stream + SC.chunk_off[S.chunk0], SC.chunk_len[S.chunk0] * 4u, &bar[0]);
+  }
+
   float2* sp = nullptr;
   float2* sq = nullptr;
   uint32_t* sab = nullptr;
   float* srest = nullptr;
   float* sstiff = nullptr;
   if (SMEM) {
-    unsigned char* base = smem + (size_t)g * region_bytes;
     sp = reinterpret_cast<float2*>(base);
     sq = sp + B.np;
     sab = reinterpret_cast<uint32_t*>(sq + (FULL ? B.np : 0));
@@ -143,11 +209,10 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
       srest[i] = grest[i];
       sstiff[i] = gstiff[i];
     }
-    group_sync(g, T);
   }
+  group_sync(g, T);
 
   auto run = [&](uint32_t op) {
-    if (op == B2D_NONE) return;
     if (op & OP_INTEG) {
       const uint32_t i = op & ~OP_INTEG;
       float2* pp = SMEM ? sp + i : gp + bidx[i];
@@ -181,22 +246,37 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     }
   };
 
-  const DSched S = SC.scheds[B.sched];
-  const uint32_t* __restrict__ lv = SC.lvl + S.lvl0;
-  const uint32_t* __restrict__ ops = SC.ops + S.op0;
-  const uint32_t nl = S.nlvl;
-  auto lvat = [&](uint32_t i) { return __ldg(lv + (i < nl ? i : nl)); };
-  uint32_t b0 = 0, e0 = lvat(1), e1 = lvat(2), e2 = lvat(3);
-  uint32_t o0 = (b0 + t < e0) ? __ldg(ops + b0 + t) : B2D_NONE;
-  uint32_t o1 = (e0 + t < e1) ? __ldg(ops + e0 + t) : B2D_NONE;
-  for (uint32_t l = 0; l < nl; ++l) {
-    const uint32_t o2 = (e1 + t < e2) ? __ldg(ops + e1 + t) : B2D_NONE;
-    const uint32_t e3 = lvat(l + 4);
-    run(o0);
-    for (uint32_t k = b0 + t + T; k < e0; k += T) run(__ldg(ops + k));
+  // buffer k2 = c & 1 is used for the (c >> 1)-th time: its mbarrier phase
+  // parity is (c >> 1) & 1
+  for (uint32_t c = 0; c < S.nchunks; ++c) {
+    const uint32_t k2 = c & 1u;
+    const uint32_t par = (c >> 1) & 1u;
+    uint32_t* buf = cbuf + k2 * SCHED_CHUNK_WORDS;
+    if (t == 0) *flag = mbar_wait_bounded(&bar[k2], par) ? 1u : 0u;
     group_sync(g, T);
-    b0 = e0; e0 = e1; e1 = e2; e2 = e3;
-    o0 = o1; o1 = o2;
+    if (*flag == 0u) {
+      if (t == 0) {
+        atomicOr(SC.err, ERR_BIT_TMA_TIMEOUT);
+        mbar_wait_bounded(&bar[k2], par);  // let the copy in flight land
+      }
+      return;  // every thread of the group leaves together
+    }
+    mbar_try(&bar[k2], par);  // completed phase: makes the data visible here
+    if (t == 0 && c + 1 < S.nchunks) {
+      fence_proxy_async();
+      bulk_load(cbuf + (k2 ^ 1u) * SCHED_CHUNK_WORDS, SC.stream + SC.chunk_off[S.chunk0 + c + 1],
+                SC.chunk_len[S.chunk0 + c + 1] * 4u, &bar[k2 ^ 1u]);
+    }
+    const uint32_t nseg = buf[0];
+    const uint32_t* ends = buf + 1;
+    const uint32_t* ops = buf + 1 + nseg;
+    uint32_t beg = 0;
+    for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
+      const uint32_t end = ends[sgi];
+      for (uint32_t k = beg + t; k < end; k += T) run(ops[k]);
+      group_sync(g, T);
+      beg = end;
+    }
   }
 
   if (SMEM) {
@@ -401,14 +481,87 @@ __device__ __forceinline__ uint32_t stage_of(const uint32_t* so, uint32_t nstage
   return lo;
 }
 
+// Circle and polygon arrays of one world, in global or shared memory.
+struct RigidView {
+  float2* cp; float2* cq; float2* ca; float* cr; uint32_t* cst;
+  uint2* clab; float* clrest;
+  DPoly* polys; float2* vpos; float2* vprev; float2* vacc; float2* pcenter; float4* paabb;
+  uint2* plab; float* plrest; uint32_t* stage_off;
+  uint32_t nc, ncl, ng, nv, npl, nst;
+};
+
+__device__ __forceinline__ RigidView global_view(const DWorld& W) {
+  RigidView v;
+  v.cp = W.cpos; v.cq = W.cprev; v.ca = W.cacc; v.cr = W.crad; v.cst = W.cstatic;
+  v.clab = W.clab; v.clrest = W.clrest;
+  v.polys = W.polys; v.vpos = W.vpos; v.vprev = W.vprev; v.vacc = W.vacc;
+  v.pcenter = W.pcenter; v.paabb = W.paabb; v.plab = W.plab; v.plrest = W.plrest;
+  v.stage_off = W.stage_off;
+  v.nc = W.nc; v.ncl = W.ncl; v.ng = W.ng;
+  v.nv = W.ng ? W.polys[W.ng - 1].v0 + W.polys[W.ng - 1].nv : 0u;
+  v.npl = W.ng ? W.polys[W.ng - 1].l0 + W.polys[W.ng - 1].nl : 0u;
+  v.nst = W.ng >= 2 ? W.ng * (W.ng - 1) + 1 : 0u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t rigid_smem_bytes(const RigidView& v) {
+  // payload plus 16-byte rounding of the 16 pieces (stage_view)
+  return 48u * v.ng + 28u * v.nc + 12u * v.ncl + 24u * v.nv + 12u * v.npl + 4u * v.nst + 256u;
+}
+
+// carve a shared-memory view (16-byte aligned pieces first)
+__device__ __forceinline__ RigidView stage_view(const RigidView& g, unsigned char* sm) {
+  RigidView v = g;
+  unsigned char* p = sm;
+  auto take = [&](size_t bytes) { unsigned char* q = p; p += (bytes + 15) & ~(size_t)15; return q; };
+  v.paabb = reinterpret_cast<float4*>(take(16u * g.ng));
+  v.polys = reinterpret_cast<DPoly*>(take(24u * g.ng));
+  v.pcenter = reinterpret_cast<float2*>(take(8u * g.ng));
+  v.cp = reinterpret_cast<float2*>(take(8u * g.nc));
+  v.cq = reinterpret_cast<float2*>(take(8u * g.nc));
+  v.ca = reinterpret_cast<float2*>(take(8u * g.nc));
+  v.vpos = reinterpret_cast<float2*>(take(8u * g.nv));
+  v.vprev = reinterpret_cast<float2*>(take(8u * g.nv));
+  v.vacc = reinterpret_cast<float2*>(take(8u * g.nv));
+  v.clab = reinterpret_cast<uint2*>(take(8u * g.ncl));
+  v.plab = reinterpret_cast<uint2*>(take(8u * g.npl));
+  v.cr = reinterpret_cast<float*>(take(4u * g.nc));
+  v.cst = reinterpret_cast<uint32_t*>(take(4u * g.nc));
+  v.clrest = reinterpret_cast<float*>(take(4u * g.ncl));
+  v.plrest = reinterpret_cast<float*>(take(4u * g.npl));
+  v.stage_off = reinterpret_cast<uint32_t*>(take(4u * g.nst));
+  return v;
+}
+
+// copy a view's arrays: everything when `all`, else only the mutable state
+__device__ __forceinline__ void copy_view(const RigidView& d, const RigidView& s, bool all) {
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  for (uint32_t i = tid; i < s.nc; i += nt) {
+    d.cp[i] = s.cp[i]; d.cq[i] = s.cq[i]; d.ca[i] = s.ca[i];
+    if (all) { d.cr[i] = s.cr[i]; d.cst[i] = s.cst[i]; }
+  }
+  for (uint32_t i = tid; i < s.nv; i += nt) {
+    d.vpos[i] = s.vpos[i]; d.vprev[i] = s.vprev[i]; d.vacc[i] = s.vacc[i];
+  }
+  for (uint32_t i = tid; i < s.ng; i += nt) {
+    d.pcenter[i] = s.pcenter[i]; d.paabb[i] = s.paabb[i];
+    if (all) d.polys[i] = s.polys[i];
+  }
+  if (all) {
+    for (uint32_t i = tid; i < s.ncl; i += nt) { d.clab[i] = s.clab[i]; d.clrest[i] = s.clrest[i]; }
+    for (uint32_t i = tid; i < s.npl; i += nt) { d.plab[i] = s.plab[i]; d.plrest[i] = s.plrest[i]; }
+    for (uint32_t i = tid; i < s.nst; i += nt) d.stage_off[i] = s.stage_off[i];
+  }
+}
+
 // gravity + links + circle pairs + polygon pairs of one sub-step for the
 // circles and polygons (src/solver.rs:110-112)
-__device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
+__device__ __forceinline__ void rigid_phase_a(const DWorld& W, const RigidView& R, bool want_aabb) {
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
-  float2* cp = W.cpos;
-  float2* ca = W.cacc;
-  const float* cr = W.crad;
-  const DPoly* polys = W.polys;
+  float2* cp = R.cp;
+  float2* ca = R.ca;
+  const float* cr = R.cr;
+  const DPoly* polys = R.polys;
   __shared__ uint32_t s_first;
   // gravity, src/solver.rs:130-141 (static bodies included)
   for (uint32_t i = tid; i < W.nc; i += nt) {
@@ -419,9 +572,9 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
   for (uint32_t g = 0; g < W.ng; ++g) {
     const DPoly P = polys[g];
     for (uint32_t v = tid; v < P.nv; v += nt) {
-      float2 a = W.vacc[P.v0 + v];
+      float2 a = R.vacc[P.v0 + v];
       a.x = fadd(a.x, W.gx); a.y = fadd(a.y, W.gy);
-      W.vacc[P.v0 + v] = a;
+      R.vacc[P.v0 + v] = a;
     }
   }
   __syncthreads();
@@ -429,22 +582,22 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
   for (uint32_t it = 0; it < W.I; ++it) {
     if (tid == 0) {
       for (uint32_t k = 0; k < W.ncl; ++k) {
-        const uint2 e = W.clab[k];
+        const uint2 e = R.clab[k];
         float2 pa = cp[e.x], pb = cp[e.y];
-        circle_link_solve(pa, cr[e.x], pb, cr[e.y], W.clrest[k]);
+        circle_link_solve(pa, cr[e.x], pb, cr[e.y], R.clrest[k]);
         cp[e.x] = pa; cp[e.y] = pb;
       }
     }
     for (uint32_t g = tid; g < W.ng; g += nt) {  // one thread per polygon
       const DPoly P = polys[g];
-      float2* v = W.vpos + P.v0;
+      float2* v = R.vpos + P.v0;
       float2 c;
       calc_center(v, P.nv, c);  // Polygon::solve_links, src/polygon.rs:218-223
-      W.pcenter[g] = c;
+      R.pcenter[g] = c;
       for (uint32_t k = 0; k < P.nl; ++k) {
-        const uint2 e = W.plab[P.l0 + k];
+        const uint2 e = R.plab[P.l0 + k];
         float2 pa = v[e.x], pb = v[e.y];
-        link_solve(pa, pb, W.plrest[P.l0 + k], 1.0f);
+        link_solve(pa, pb, R.plrest[P.l0 + k], 1.0f);
         v[e.x] = pa; v[e.y] = pb;
       }
     }
@@ -483,7 +636,7 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
   // polygon pairs, src/solver.rs:178-187 + src/polygon.rs:142-216
   const uint32_t nstage = W.ng >= 2 ? W.ng * (W.ng - 1) : 0;
   if (nstage > 0) {
-    const uint32_t* so = W.stage_off;
+    const uint32_t* so = R.stage_off;
     const uint32_t total = so[nstage];
     uint32_t start = 0;
     while (start < total) {
@@ -500,8 +653,8 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
         const uint32_t q = r - e * PO.nv;
         const uint32_t b = (e + 1) % PS.nv;
         float2 na, nb, nq;
-        if (resolve_line(W.pcenter[self], W.vpos[PS.v0 + e], W.vpos[PS.v0 + b],
-                         W.vpos[PO.v0 + q], W.pcenter[other], na, nb, nq))
+        if (resolve_line(R.pcenter[self], R.vpos[PS.v0 + e], R.vpos[PS.v0 + b],
+                         R.vpos[PO.v0 + q], R.pcenter[other], na, nb, nq))
           atomicMin(&s_first, x);
       }
       __syncthreads();
@@ -521,14 +674,14 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
         const DPoly PS = polys[self], PO = polys[other];
         const uint32_t e = (f - so[st]) / PO.nv;
         const uint32_t b = (e + 1) % PS.nv;
-        const float2 pa = W.vpos[PS.v0 + e], pb = W.vpos[PS.v0 + b];
-        const float2 sc = W.pcenter[self], oc = W.pcenter[other];
+        const float2 pa = R.vpos[PS.v0 + e], pb = R.vpos[PS.v0 + b];
+        const float2 sc = R.pcenter[self], oc = R.pcenter[other];
         for (uint32_t q = 0; q < PO.nv; ++q) {
           float2 na, nb, nq;
-          if (resolve_line(sc, pa, pb, W.vpos[PO.v0 + q], oc, na, nb, nq)) {
-            W.vpos[PS.v0 + e] = na;
-            W.vpos[PS.v0 + b] = nb;
-            W.vpos[PO.v0 + q] = nq;
+          if (resolve_line(sc, pa, pb, R.vpos[PO.v0 + q], oc, na, nb, nq)) {
+            R.vpos[PS.v0 + e] = na;
+            R.vpos[PS.v0 + b] = nb;
+            R.vpos[PO.v0 + q] = nq;
           }
         }
         s_first = so[st] + (e + 1) * PO.nv;  // first test of the next edge step
@@ -542,7 +695,7 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
   if (want_aabb) {
     for (uint32_t g = tid; g < W.ng; g += nt) {
       const DPoly P = polys[g];
-      const float2* v = W.vpos + P.v0;
+      const float2* v = R.vpos + P.v0;
       float4 bb = make_float4(0.f, 0.f, 0.f, 0.f);
       if (P.nv > 0) {
         bb = make_float4(v[0].x, v[0].y, v[0].x, v[0].y);
@@ -553,7 +706,7 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
           if (v[i].y > bb.w) bb.w = v[i].y;
         }
       }
-      W.paabb[g] = bb;
+      R.paabb[g] = bb;
     }
   }
   __syncthreads();
@@ -561,13 +714,13 @@ __device__ void rigid_phase_a(const DWorld& W, bool want_aabb) {
 
 // bounds + integrate of one sub-step for the circles and polygons
 // (src/solver.rs:113-114)
-__device__ void rigid_phase_b(const DWorld& W) {
+__device__ __forceinline__ void rigid_phase_b(const DWorld& W, const RigidView& R) {
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
-  float2* cp = W.cpos;
-  float2* cq = W.cprev;
-  float2* ca = W.cacc;
-  const float* cr = W.crad;
-  const DPoly* polys = W.polys;
+  float2* cp = R.cp;
+  float2* cq = R.cq;
+  float2* ca = R.ca;
+  const float* cr = R.cr;
+  const DPoly* polys = R.polys;
   // bounds, src/solver.rs:155-165
   for (uint32_t i = tid; i < W.nc; i += nt) {
     float2 p = cp[i], q = cq[i];
@@ -577,15 +730,15 @@ __device__ void rigid_phase_b(const DWorld& W) {
   for (uint32_t g = 0; g < W.ng; ++g) {
     const DPoly P = polys[g];
     for (uint32_t v = tid; v < P.nv; v += nt) {
-      float2 p = W.vpos[P.v0 + v], q = W.vprev[P.v0 + v];
+      float2 p = R.vpos[P.v0 + v], q = R.vprev[P.v0 + v];
       solve_bounds(p, q, W);
-      W.vpos[P.v0 + v] = p; W.vprev[P.v0 + v] = q;
+      R.vpos[P.v0 + v] = p; R.vprev[P.v0 + v] = q;
     }
   }
   __syncthreads();
   // update_positions, src/solver.rs:118-128
   for (uint32_t i = tid; i < W.nc; i += nt) {
-    if (W.cstatic[i]) continue;  // extension: static circle
+    if (R.cst[i]) continue;  // extension: static circle
     float2 p = cp[i], q = cq[i];
     const float2 a = ca[i];
     integrate(p, q, a.x, a.y, W.h);
@@ -595,19 +748,19 @@ __device__ void rigid_phase_b(const DWorld& W) {
     const DPoly P = polys[g];
     if (P.is_static) continue;
     float2 c;
-    calc_center(W.vpos + P.v0, P.nv, c);
-    W.pcenter[g] = c;
+    calc_center(R.vpos + P.v0, P.nv, c);
+    R.pcenter[g] = c;
   }
   __syncthreads();
   for (uint32_t g = 0; g < W.ng; ++g) {
     const DPoly P = polys[g];
     if (P.is_static) continue;
     for (uint32_t v = tid; v < P.nv; v += nt) {
-      float2 p = W.vpos[P.v0 + v], q = W.vprev[P.v0 + v];
-      const float2 a = W.vacc[P.v0 + v];
+      float2 p = R.vpos[P.v0 + v], q = R.vprev[P.v0 + v];
+      const float2 a = R.vacc[P.v0 + v];
       integrate(p, q, a.x, a.y, W.h);
-      W.vpos[P.v0 + v] = p; W.vprev[P.v0 + v] = q;
-      W.vacc[P.v0 + v] = make_float2(0.0f, 0.0f);
+      R.vpos[P.v0 + v] = p; R.vprev[P.v0 + v] = q;
+      R.vacc[P.v0 + v] = make_float2(0.0f, 0.0f);
     }
   }
   __syncthreads();
@@ -615,36 +768,53 @@ __device__ void rigid_phase_b(const DWorld& W) {
 
 // MODE 0: the whole Solver::update step; 1: phase A of sub-step `sub`;
 // 2: phase B of sub-step `sub`; 3: phase B of `sub`-1, then phase A of `sub`.
+// The world's circles and polygons are staged in shared memory when they fit
+// in `smem_bytes` (serial chains then cost shared-memory latency), else the
+// phases run on global memory.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_rigid(const DWorld* __restrict__ worlds,
+__global__ void __launch_bounds__(128) k_rigid(const DWorld* __restrict__ worlds,
                                                const uint32_t* __restrict__ wlist, uint32_t n,
-                                               uint32_t sub) {
+                                               uint32_t sub, uint32_t smem_bytes) {
+  extern __shared__ __align__(16) unsigned char rsm[];
   if (blockIdx.x >= n) return;
   const DWorld& W = worlds[wlist[blockIdx.x]];
+  if (MODE == 1 && sub >= W.S) return;
+  if (MODE == 2 && sub >= W.S) return;
+  if (MODE == 3 && sub > W.S) return;
   const bool aabb = (W.flags & COLLIDE_PPOLY) != 0;
+  RigidView G = global_view(W);
+  RigidView R = G;
+  const bool staged = rigid_smem_bytes(G) <= smem_bytes;
+  if (staged) {
+    R = stage_view(G, rsm);
+    copy_view(R, G, true);
+    __syncthreads();
+  }
   if (MODE == 0) {
     for (uint32_t s = 0; s < W.S; ++s) {
-      rigid_phase_a(W, false);
-      rigid_phase_b(W);
+      rigid_phase_a(W, R, false);
+      rigid_phase_b(W, R);
     }
   } else if (MODE == 1) {
-    if (sub < W.S) rigid_phase_a(W, aabb);
+    rigid_phase_a(W, R, aabb);
   } else if (MODE == 2) {
-    if (sub < W.S) rigid_phase_b(W);
+    rigid_phase_b(W, R);
   } else {
-    if (sub >= 1 && sub - 1 < W.S) rigid_phase_b(W);
-    if (sub < W.S) rigid_phase_a(W, aabb);
+    if (sub >= 1 && sub - 1 < W.S) rigid_phase_b(W, R);
+    if (sub < W.S) rigid_phase_a(W, R, aabb);
+  }
+  if (staged) {
+    __syncthreads();
+    copy_view(G, R, false);
   }
 }
 
 // ----------------------------------------------------------------------------
 // Extension: particle collisions (not in the reference, whose solver
 // particles only interact through links, src/solver.rs:143-188).  Hashed
-// uniform grid: bucket = hash(world, cell) & mask with BUCKET_K slots per
-// bucket plus an overflow list.  For each particle, neighbour cells are
-// visited dy outer, dx inner (-1..1) and, within a cell, particles in
-// ascending index: the Jacobi sum order is fixed by the spec, not by hashing
-// or by the order of atomics.
+// uniform grid (counting sort per sub-step); Jacobi contacts against every
+// particle of the 9 surrounding cells, summed in fixed point so that the
+// result does not depend on the visiting order.
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell) {
   float v = floorf(fdiv(fsub(p, origin), cell));
@@ -652,19 +822,22 @@ __device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell)
   if (v > 1.0e9f) v = 1.0e9f;
   return (int32_t)v;
 }
-__device__ __forceinline__ uint32_t cell_hash(uint32_t w, int32_t cx, int32_t cy, uint32_t mask) {
-  uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u) ^ (w * 83492791u);
+__device__ __forceinline__ uint32_t cell_hash(int32_t cx, int32_t cy) {
+  uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u);
   h ^= h >> 15;
   h *= 0x2c1b3c6du;
   h ^= h >> 12;
-  return h & mask;
+  return h;
 }
 
 constexpr uint32_t CHUNK = 256;  // particles per work chunk (one CTA)
 
-__global__ void __launch_bounds__(CHUNK) k_grid_insert(const DWorld* __restrict__ worlds, DGrid G,
-                                                       const uint2* __restrict__ chunks,
-                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
+// Bucket entry: {pos.x bits, pos.y bits, particle index, cell x}.  An entry
+// belongs to cell (cx, cy) when its stored cell x equals cx and the cell y
+// recomputed from the stored pos.y equals cy: exact, whatever the hashing.
+__global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __restrict__ worlds, DGrid G,
+                                                      const uint2* __restrict__ chunks,
+                                                      uint32_t nchunks, uint32_t cur, uint32_t sub) {
   if (blockIdx.x >= nchunks) return;
   const uint2 ch = chunks[blockIdx.x];
   const DWorld& W = worlds[ch.x];
@@ -672,30 +845,111 @@ __global__ void __launch_bounds__(CHUNK) k_grid_insert(const DWorld* __restrict_
   if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
   const float2 p = W.pos[cur][j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
-  const uint32_t b = cell_hash(ch.x, cx, cy, G.mask);
-  const uint32_t s = atomicAdd(&G.count[b], 1u);
-  const uint4 ent = make_uint4(ch.x, j, (uint32_t)cx, (uint32_t)cy);
-  if (s < BUCKET_K) {
-    G.slots[(size_t)b * BUCKET_K + s] = ent;
-  } else {
-    const uint32_t o = atomicAdd(&G.ovf_n[0], 1u);
-    if (o < G.ovf_cap) {  // capacity = all particles, so this always holds
-      G.overflow[o] = ent;
-      G.ovf_bucket[o] = b;
+  const uint32_t b = W.gb0 + (cell_hash(cx, cy) & W.gmask);
+  const uint32_t r = atomicAdd(&G.count[b], 1u);
+  G.pbr[W.gp0 + j] = make_uint2(b, r);
+}
+
+// block-wide exclusive scan of one value per thread (blockDim = 1024)
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sum[32];
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) warp_sum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t nw = blockDim.x >> 5;
+    uint32_t w = lane < nw ? warp_sum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= (uint32_t)o) w += y;
     }
+    warp_sum[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  const uint32_t before = wid ? warp_sum[wid - 1] : 0u;
+  if (total) *total = warp_sum[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// sum of each SCAN_TILE counts
+__global__ void __launch_bounds__(1024) k_scan_reduce(DGrid G, uint32_t nbuckets) {
+  const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * 4u;
+  uint32_t v = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k)
+    if (base + k < nbuckets) v += G.count[base + k];
+  uint32_t tot;
+  block_exclusive_scan(v, &tot);
+  if (threadIdx.x == 0) G.partial[blockIdx.x] = tot;
+}
+
+// start[b] = exclusive prefix sum of count (tile offset from the partials)
+__global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets) {
+  __shared__ uint32_t s_off;
+  // offset of this tile: sum of the partials of the tiles before it
+  uint32_t acc = 0;
+  for (uint32_t t = threadIdx.x; t < blockIdx.x; t += blockDim.x) acc += G.partial[t];
+  uint32_t tot;
+  block_exclusive_scan(acc, &tot);
+  if (threadIdx.x == 0) s_off = tot;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * 4u;
+  uint32_t c[4], v = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    c[k] = base + k < nbuckets ? G.count[base + k] : 0u;
+    v += c[k];
+  }
+  uint32_t run = s_off + block_exclusive_scan(v, nullptr);
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    if (base + k < nbuckets) G.start[base + k] = run;
+    run += c[k];
   }
 }
 
-__device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D2, float& ddx,
-                                           float& ddy, bool& hit) {
+__global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __restrict__ worlds, DGrid G,
+                                                        const uint2* __restrict__ chunks,
+                                                        uint32_t nchunks, uint32_t cur,
+                                                        uint32_t sub) {
+  if (blockIdx.x >= nchunks) return;
+  const uint2 ch = chunks[blockIdx.x];
+  const DWorld& W = worlds[ch.x];
+  const uint32_t j = ch.y + threadIdx.x;
+  if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
+  const float2 p = W.pos[cur][j];
+  const uint2 br = G.pbr[W.gp0 + j];
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell);
+  G.sorted[G.start[br.x] + br.y] =
+      make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), j, (uint32_t)cx);
+}
+
+// Contact corrections are summed in 64-bit fixed point (units of 2^-32,
+// round to nearest even), which makes the sum independent of the order in
+// which neighbours are found.
+__device__ __forceinline__ long long fix32(float c) { return __float2ll_rn(fmul(c, 4294967296.0f)); }
+__device__ __forceinline__ float unfix32(long long s) {
+  return __double2float_rn(__dmul_rn(__ll2double_rn(s), 2.3283064365386962890625e-10));
+}
+
+__device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D2, long long& sx,
+                                           long long& sy, bool& hit) {
   const float dx = fsub(p.x, pj.x), dy = fsub(p.y, pj.y);
   const float d2 = fadd(fmul(dx, dx), fmul(dy, dy));
   if (d2 < D2 && d2 > 0.0f) {
     const float dist = fsqrt(d2);
     const float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
     const float ov = fsub(D, dist);
-    ddx = fadd(ddx, fmul(fmul(nx, ov), 0.5f));
-    ddy = fadd(ddy, fmul(fmul(ny, ov), 0.5f));
+    sx += fix32(fmul(fmul(nx, ov), 0.5f));
+    sy += fix32(fmul(fmul(ny, ov), 0.5f));
     hit = true;
   }
 }
@@ -767,10 +1021,24 @@ __device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p) {
   return p;
 }
 
+// Contacts of particle i with the particles of cell (ncx, ncy), stored in
+// bucket b.
+__device__ __forceinline__ void visit_cell(const DGrid& G, const DWorld& W, uint32_t i, float2 p,
+                                           int32_t ncx, int32_t ncy, uint32_t s0, uint32_t cnt,
+                                           float D, float D2, long long& sx, long long& sy,
+                                           bool& hit) {
+  for (uint32_t k = s0; k < s0 + cnt; ++k) {
+    const uint4 e = G.sorted[k];
+    if (e.w != (uint32_t)ncx || e.z == i) continue;
+    if (cell_coord(__uint_as_float(e.y), W.by, W.cell) != ncy) continue;
+    pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, sx, sy, hit);
+  }
+}
+
 // Particle collisions + bounds + integrate of one sub-step of the extension
 // pipeline.  Reads positions from buffer cur (the post-link snapshot) and
 // writes the new ones to buffer cur^1; prev is updated in place.
-__global__ void __launch_bounds__(CHUNK) k_collide_integrate(const DWorld* __restrict__ worlds,
+__global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __restrict__ worlds,
                                                              DGrid G, const uint2* __restrict__ chunks,
                                                              uint32_t nchunks, uint32_t cur,
                                                              uint32_t sub) {
@@ -786,46 +1054,30 @@ __global__ void __launch_bounds__(CHUNK) k_collide_integrate(const DWorld* __res
     const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
     const float D = fadd(W.radius, W.radius);
     const float D2 = fmul(D, D);
-    const uint32_t novf = min(G.ovf_n[0], G.ovf_cap);
-    float ddx = 0.0f, ddy = 0.0f;
+    long long sx = 0, sy = 0;
     bool hit = false;
-    for (int dy = -1; dy <= 1; ++dy) {
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int32_t ncx = cx + dx, ncy = cy + dy;
-        const uint32_t b = cell_hash(ch.x, ncx, ncy, G.mask);
-        const uint32_t cnt = G.count[b];
-        if (cnt == 0) continue;
-        const uint32_t nk = cnt < BUCKET_K ? cnt : BUCKET_K;
-        const uint4* sl = G.slots + (size_t)b * BUCKET_K;
-        // matching entries in ascending particle index (selection order)
-        uint32_t last = 0;
-        bool have_last = false;
-        for (;;) {
-          uint32_t best = 0xFFFFFFFFu;
-          for (uint32_t s = 0; s < nk; ++s) {
-            const uint4 e = sl[s];
-            if (e.x != ch.x || (int32_t)e.z != ncx || (int32_t)e.w != ncy) continue;
-            if (have_last && e.y <= last) continue;
-            if (e.y < best) best = e.y;
-          }
-          if (cnt > BUCKET_K) {
-            for (uint32_t o = 0; o < novf; ++o) {
-              if (G.ovf_bucket[o] != b) continue;
-              const uint4 e = G.overflow[o];
-              if (e.x != ch.x || (int32_t)e.z != ncx || (int32_t)e.w != ncy) continue;
-              if (have_last && e.y <= last) continue;
-              if (e.y < best) best = e.y;
-            }
-          }
-          if (best == 0xFFFFFFFFu) break;
-          last = best;
-          have_last = true;
-          if (best == i) continue;
-          pp_contact(p, P[best], D, D2, ddx, ddy, hit);
-        }
-      }
-    }
-    if (hit) { p.x = fadd(p.x, ddx); p.y = fadd(p.y, ddy); }
+    // the nine buckets' ranges are loaded together, then scanned
+#define B2D_BK(c) (W.gb0 + (cell_hash(cx + ((c) % 3) - 1, cy + ((c) / 3) - 1) & W.gmask))
+    const uint32_t b0 = B2D_BK(0), b1 = B2D_BK(1), b2 = B2D_BK(2), b3 = B2D_BK(3),
+                   b4 = B2D_BK(4), b5 = B2D_BK(5), b6 = B2D_BK(6), b7 = B2D_BK(7),
+                   b8 = B2D_BK(8);
+#undef B2D_BK
+    const uint32_t n0 = G.count[b0], n1 = G.count[b1], n2 = G.count[b2], n3 = G.count[b3],
+                   n4 = G.count[b4], n5 = G.count[b5], n6 = G.count[b6], n7 = G.count[b7],
+                   n8 = G.count[b8];
+    const uint32_t s0 = G.start[b0], s1 = G.start[b1], s2 = G.start[b2], s3 = G.start[b3],
+                   s4 = G.start[b4], s5 = G.start[b5], s6 = G.start[b6], s7 = G.start[b7],
+                   s8 = G.start[b8];
+    visit_cell(G, W, i, p, cx - 1, cy - 1, s0, n0, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy - 1, s1, n1, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy - 1, s2, n2, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx - 1, cy, s3, n3, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy, s4, n4, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy, s5, n5, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx - 1, cy + 1, s6, n6, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy + 1, s7, n7, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy + 1, s8, n8, D, D2, sx, sy, hit);
+    if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
   }
   if (W.flags & COLLIDE_PC) p = particle_circles(W, p);
   if (W.flags & COLLIDE_PPOLY) {

@@ -69,23 +69,54 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   std::vector<uint32_t> start(maxl + 2, 0);
   for (uint32_t l : lvl_of) start[l + 1]++;
   for (uint32_t l = 1; l <= maxl + 1; ++l) start[l] += start[l - 1];
-  DSched d;
-  d.lvl0 = (uint32_t)lvl.size();
-  d.nlvl = maxl;
-  d.op0 = (uint32_t)ops.size();
-  d.nops = (uint32_t)total;
-  for (uint32_t l = 1; l <= maxl + 1; ++l) lvl.push_back(start[l]);  // lv[l-1] = begin of level l
-  ops.resize(ops.size() + total);
-  uint32_t* dst = ops.data() + d.op0;
-  std::vector<uint32_t> fill(start.begin(), start.end());
-  for (size_t i = 0; i < total; ++i) dst[fill[lvl_of[i]]++] = op_of[i];
-  // self-check: every op names a link or particle of the body, and the level
-  // offsets cover the op list exactly
-  for (size_t i = 0; i < total; ++i) {
-    const uint32_t op = dst[i];
+  std::vector<uint32_t> sorted(total);
+  {
+    std::vector<uint32_t> fill(start.begin(), start.end());
+    for (size_t i = 0; i < total; ++i) sorted[fill[lvl_of[i]]++] = op_of[i];
+  }
+  for (size_t i = 0; i < total; ++i) {  // self-check: ops name the body's links/particles
+    const uint32_t op = sorted[i];
     if ((op & OP_INTEG) ? (op & ~OP_INTEG) >= np : op >= nl) std::abort();
   }
-  if (lvl.back() != total) std::abort();
+  // cut the level sequence into chunks (a level may span chunks)
+  DSched d;
+  d.chunk0 = (uint32_t)chunk_off.size();
+  d.nlvl = maxl;
+  d.nops = (uint32_t)total;
+  std::vector<uint32_t> seg_end, chunk_ops;
+  auto flush = [&]() {
+    if (seg_end.empty()) return;
+    while (stream.size() % 4) stream.push_back(0);
+    chunk_off.push_back((uint32_t)stream.size());
+    const size_t at = stream.size();
+    stream.push_back((uint32_t)seg_end.size());
+    stream.insert(stream.end(), seg_end.begin(), seg_end.end());
+    stream.insert(stream.end(), chunk_ops.begin(), chunk_ops.end());
+    while ((stream.size() - at) % 4) stream.push_back(0);
+    chunk_len.push_back((uint32_t)(stream.size() - at));
+    if (chunk_len.back() > SCHED_CHUNK_WORDS) std::abort();
+    seg_end.clear();
+    chunk_ops.clear();
+  };
+  for (uint32_t l = 1; l <= maxl; ++l) {
+    uint32_t b = start[l];
+    const uint32_t e = start[l + 1];
+    while (b < e) {
+      // words used: 1 (nseg) + segments + ops, plus 1 for this segment, padded to 4
+      size_t used = 1 + seg_end.size() + chunk_ops.size();
+      size_t room = SCHED_CHUNK_WORDS - 3 - used - 1;
+      if (used + 1 + 1 + 3 > SCHED_CHUNK_WORDS) {
+        flush();
+        continue;
+      }
+      const uint32_t take = (uint32_t)std::min<size_t>(room, e - b);
+      chunk_ops.insert(chunk_ops.end(), sorted.begin() + b, sorted.begin() + b + take);
+      seg_end.push_back((uint32_t)chunk_ops.size());
+      b += take;
+    }
+  }
+  flush();
+  d.nchunks = (uint32_t)chunk_off.size() - d.chunk0;
   const uint32_t id = (uint32_t)scheds.size();
   scheds.push_back(d);
   index.emplace(std::move(key), id);
@@ -123,8 +154,7 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
     const DBody& B = im.bodies[g.body];
     if (B.sched >= reg.scheds.size()) return bad("schedule id");
     const DSched& S = reg.scheds[B.sched];
-    if ((size_t)S.op0 + S.nops > reg.ops.size() || (size_t)S.lvl0 + S.nlvl + 1 > reg.lvl.size())
-      return bad("schedule range");
+    if ((size_t)S.chunk0 + S.nchunks > reg.chunk_off.size()) return bad("schedule range");
     if (g.smem && !B.local) return bad("shared-memory body without local links");
     if (g.T < 32 || g.T % 32) return bad("group size");
   }

@@ -288,10 +288,16 @@ static size_t cell_lower(const CellEnt* e, size_t n, int32_t cy, int32_t cx) {
   return lo;
 }
 
-/* particle-particle: Jacobi over the pre-collision snapshot.  For particle i,
- * neighbours are visited by cell (dy outer, dx inner, each -1..1) and, within a
- * cell, by ascending particle index.  Contact when 0 < |d|^2 < (2r)^2:
- *   corr = ((d/|d|) * (2r - |d|)) * 0.5 ;  delta += corr ;  pos = pos + delta */
+/* particle-particle: Jacobi over the pre-collision snapshot.  For particle
+ * i, every other particle j whose cell is one of the 9 cells around i's cell
+ * is a candidate; contact when 0 < |d|^2 < (2r)^2, d = p_i - p_j:
+ *   corr = ((d/|d|) * (2r - |d|)) * 0.5
+ * The corrections are summed in 64-bit fixed point (units of 2^-32, each
+ * component rounded to nearest-even), so the sum does not depend on the order
+ * neighbours are visited in; then pos = pos + (float)(sum * 2^-32). */
+static int64_t fix32(float c) { return llrintf(c * 4294967296.0f); }
+static float unfix32(int64_t s) { return (float)((double)s * 0x1p-32); }
+
 static void ext_collide_pp(orc_world* w) {
   size_t n = w->np;
   if (n == 0) return;
@@ -310,7 +316,7 @@ static void ext_collide_pp(orc_world* w) {
   float D2 = D * D;
   for (size_t i = 0; i < n; ++i) {
     V2 p = snap[i];
-    V2 delta = v2(0.0f, 0.0f);
+    int64_t sx = 0, sy = 0;
     int hit = 0;
     for (int dy = -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
@@ -325,13 +331,14 @@ static void ext_collide_pp(orc_world* w) {
             float dist = sqrtf(d2);
             V2 nrm = vdiv(d, dist);
             V2 corr = vmul(vmul(nrm, D - dist), 0.5f);
-            delta = vadd(delta, corr);
+            sx += fix32(corr.x);
+            sy += fix32(corr.y);
             hit = 1;
           }
         }
       }
     }
-    if (hit) w->particles[i].pos = vadd(p, delta);
+    if (hit) w->particles[i].pos = vadd(p, v2(unfix32(sx), unfix32(sy)));
   }
   free(snap); free(ent); free(sorted);
 }
