@@ -81,6 +81,7 @@ SIGNATURES = {
     "b2d_set_mode": [_P, C.c_int],
     "b2d_set_collision": [_P, C.c_uint32, C.c_float, C.c_float],
     "b2d_set_circle_static": [_P, C.c_size_t, C.c_int],
+    "b2d_set_tuning": [_P, C.c_char_p, C.c_double],
     "b2d_update": [_P, C.c_float],
     "b2d_get_particle_len": [_P, _SZ],
     "b2d_get_circles_len": [_P, _SZ],

@@ -260,6 +260,11 @@ class Solver:
     def set_circle_static(self, index: int, is_static: bool) -> None:
         self._chk(self._lib.b2d_set_circle_static(self._h, index, int(is_static)))
 
+    def set_tuning(self, **kv) -> None:
+        """Executor tunables (see include/bendy2d.h b2d_set_tuning)."""
+        for k, v in kv.items():
+            self._chk(self._lib.b2d_set_tuning(self._h, k.encode(), float(v)))
+
     # ---- update (src/solver.rs:106-116)
     def update(self, dt: float) -> None:
         self._chk(self._lib.b2d_update(self._h, dt))

@@ -21,6 +21,7 @@ enum : uint32_t { COLLIDE_PP = 1u, COLLIDE_PC = 2u, COLLIDE_PPOLY = 4u };
 // Schedule op encoding: link ops carry the body-local link index; bounds +
 // integrate ops carry the body-local particle index with this bit set.
 constexpr uint32_t OP_INTEG = 0x80000000u;
+constexpr uint32_t OP_WIDE = 0xFFFFFFFFu;
 
 // A body is a set of solver particles run by one executor unit: a union of
 // whole link-connected components, so no link crosses two bodies.
@@ -41,8 +42,13 @@ struct DPoly {
 // SCHED_CHUNK_WORDS 32-bit words, each 16-byte aligned so that one bulk copy
 // (TMA, cp.async.bulk) moves it into shared memory:
 //   word 0            nseg
-//   words 1..nseg     end offset of each segment within the op list
-//   words 1+nseg..    ops of the chunk (link index, or OP_INTEG | particle)
+//   words 1..nseg     end of each segment, counted in ops
+//   (pad to an even word)
+//   then two words per op:
+//     link op    {a | b << 16, link index}   (body-local endpoints; bodies
+//                                             of up to 65535 particles)
+//                {link index, OP_WIDE}       (larger bodies)
+//     integrate  {particle, OP_INTEG}
 // A segment is a whole level or a piece of one; a group barrier follows
 // every segment.
 constexpr uint32_t SCHED_CHUNK_WORDS = 4096;
@@ -102,7 +108,7 @@ enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u };
 constexpr uint32_t SCAN_TILE = 4096;  // buckets per scan block (1024 threads x 4)
 struct DGrid {
   uint32_t* count;       // nbuckets: entries per bucket
-  uint32_t* start;       // nbuckets: exclusive prefix sum of count
+  uint2* range;          // nbuckets: {exclusive prefix sum of count, count}
   uint32_t* partial;     // per scan tile: sum of its counts
   uint2* pbr;            // per particle: (bucket, rank within bucket)
   uint4* sorted;         // per particle: {pos.x bits, pos.y bits, particle, cell x}

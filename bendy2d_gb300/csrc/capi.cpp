@@ -36,6 +36,8 @@ struct b2d_solver {
   cudaStream_t stream = nullptr;
   bool graphs = true;
   bool profiling = false;
+  PlanTuning tune;
+  bool tune_set = false;
 };
 
 struct b2d_batch {
@@ -65,6 +67,7 @@ static int engine_for(b2d_solver* s, Engine** out) {
     s->own = std::make_unique<Engine>(s->stream);
     s->own->set_use_graph(s->graphs);
     s->own->set_profile(s->profiling);
+    if (s->tune_set) s->own->set_tuning(s->tune);
   }
   *out = s->own.get();
   return OK;
@@ -329,6 +332,16 @@ int b2d_set_circle_static(b2d_solver* s, size_t i, int on) {
   if (i >= s->w.circles.size()) return fail(ERR_INDEX, "circle index out of range");
   s->topo_dirty = true;
   s->w.circles[i].is_static = on ? 1u : 0u;
+  return OK;
+}
+
+int b2d_set_tuning(b2d_solver* s, const char* key, double value) {
+  CHECK_S(s);
+  if (!key) return fail(ERR_NULL, "null key");
+  if (!s->tune.set(key, value)) return fail(ERR_ARG, std::string("unknown tunable: ") + key);
+  s->tune_set = true;
+  MUTATE(s);
+  if (s->own) s->own->set_tuning(s->tune);
   return OK;
 }
 

@@ -46,6 +46,9 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
     own_stream_ = true;
   }
+  for (auto& a : aux_) cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
+  evpool_.resize(256);
+  for (auto& e : evpool_) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   if (g_smem_optin < 0) {
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
@@ -77,6 +80,8 @@ Engine::~Engine() {
   cudaFree(d_lists_);
   cudaFree(d_wlists_);
   cudaFree(d_grid_);
+  for (auto& e : evpool_) cudaEventDestroy(e);
+  for (auto& a : aux_) cudaStreamDestroy(a);
   if (own_stream_) cudaStreamDestroy(stream_);
 }
 
@@ -98,6 +103,13 @@ void Engine::set_stream(cudaStream_t s) {
     own_stream_ = true;
   }
   invalidate_graph();
+}
+
+void Engine::set_tuning(const PlanTuning& t) {
+  const uint32_t cap = tune_.smem_max;
+  tune_ = t;
+  tune_.smem_max = std::min(tune_.smem_max, cap);
+  lists_dirty_ = true;
 }
 
 const WorldImage* Engine::image(uint32_t slot) const {
@@ -316,7 +328,7 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   const size_t ntiles = (nb + SCAN_TILE - 1) / SCAN_TILE;
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
-  const size_t o_count = seg(nb * 4), o_start = seg(nb * 4), o_part = seg(ntiles * 4),
+  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_part = seg(ntiles * 4),
                o_pbr = seg(np * 8), o_sorted = seg(np * 16);
   B2D_CUDA(cudaStreamSynchronize(stream_));
   if (d_grid_) dev_bytes_ -= grid_bytes_;
@@ -325,7 +337,7 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   B2D_CUDA(cudaMalloc(&d_grid_, bytes));
   B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
   grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
-  grid_.start = reinterpret_cast<uint32_t*>(d_grid_ + o_start);
+  grid_.range = reinterpret_cast<uint2*>(d_grid_ + o_start);
   grid_.partial = reinterpret_cast<uint32_t*>(d_grid_ + o_part);
   grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o_pbr);
   grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o_sorted);
@@ -367,7 +379,8 @@ int Engine::rebuild_lists() {
         c.region = gb.smem ? std::min<uint32_t>(rc, tune_.smem_max) : 0u;
         if (gb.smem && c.region < gb.region) c.region = gb.region;
         uint32_t G = gb.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / gb.T);
-        if (gb.T != 32) G = std::min<uint32_t>(G, 15);
+        if (gb.T != 32) G = std::min<uint32_t>(G, std::min<uint32_t>(tune_.max_groups, 15));
+        G = std::max<uint32_t>(G, 1);
         G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / (c.region + STREAM_BYTES)));
         c.G = G;
         it = cls.emplace(key, classes_.size()).first;
@@ -503,6 +516,20 @@ int Engine::launch_all(bool profiling) {
       });
     }
   };
+  // Streams: link executors, grid and collide kernels run on the main
+  // stream; circle/polygon kernels on aux streams (graph branches), joined
+  // before the collide kernel that reads them.  Profiling runs serially.
+  cudaStream_t ax = profiling ? stream_ : aux_[0];
+  cudaStream_t ax2 = profiling ? stream_ : aux_[1];
+  uint32_t evi = 0;
+  auto edge = [&](cudaStream_t a, cudaStream_t b) {
+    if (a == b) return;
+    cudaEvent_t e = evpool_[evi++ % evpool_.size()];
+    cudaEventRecord(e, a);
+    cudaStreamWaitEvent(b, e, 0);
+  };
+  edge(stream_, ax);
+  edge(stream_, ax2);
   // worlds without extension collisions: one launch per class for the whole step
   groups(true, 0, 0);
   if (!serial_full_.empty()) {
@@ -513,7 +540,7 @@ int Engine::launch_all(bool profiling) {
   }
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
-    timed("rigid_full", [&] { k_rigid<0><<<n, 128, rigid_smem_, stream_>>>(W, d_wlists_, n, 0, rigid_smem_); });
+    timed("rigid_full", [&] { k_rigid<0><<<n, 128, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
   }
   // worlds with extension collisions: per sub-step pipeline
   const uint32_t nch = (uint32_t)chunks_.size();
@@ -522,17 +549,17 @@ int Engine::launch_all(bool profiling) {
   const uint32_t* RE = d_wlists_ + off_rigid_ext_;
   for (uint32_t s = 0; s < smax_ext_; ++s) {
     const uint32_t cur = s & 1u;
+    if (nre) {  // phase B of s-1 (after collide s-1 read the circles), phase A of s
+      timed("rigid_ext", [&] {
+        if (s == 0) k_rigid<1><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        else k_rigid<3><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+      });
+    }
     groups(false, cur, s);
     if (!serial_links_.empty()) {
       const uint32_t n = (uint32_t)serial_links_.size();
       timed("exec_serial_links", [&] {
         k_exec_serial<false><<<(n + 127) / 128, 128, 0, stream_>>>(W, d_lists_ + off_serial_links_, n, cur, s);
-      });
-    }
-    if (nre) {
-      timed("rigid_ext", [&] {
-        if (s == 0) k_rigid<1><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, s, rigid_smem_);
-        else k_rigid<3><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, s, rigid_smem_);
       });
     }
     if (any_pp_) {
@@ -552,14 +579,18 @@ int Engine::launch_all(bool profiling) {
         k_grid_scatter<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });
     }
+    if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
       k_collide_integrate<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
     });
+    if (nre) edge(stream_, ax);
   }
   if (smax_ext_ > 0) {
-    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, rigid_smem_, stream_>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
+    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
     timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
   }
+  edge(ax, stream_);
+  edge(ax2, stream_);
   if (profiling) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

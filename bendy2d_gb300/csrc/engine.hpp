@@ -25,7 +25,10 @@ struct PlanTuning {
   uint32_t free_chunk = 2048;       // particles per body for link-free particles
   uint32_t smem_max = 200 * 1024;   // bytes of shared memory per group region
   uint32_t warp_groups = 8;         // groups per CTA when T == 32
-  float width_per_thread = 1.0f;    // T = pow2 >= avg width / this
+  uint32_t max_groups = 15;         // groups per CTA when T > 32
+  float width_per_thread = 0.5f;    // T = pow2 >= avg width / this (issue-bound: wide groups win)
+  // set a tunable by name; returns false for an unknown name
+  bool set(const std::string& key, double value);
 };
 
 // Engine-wide registry of level schedules, deduplicated by topology.
@@ -122,6 +125,7 @@ class Engine {
   const WorldImage* image(uint32_t slot) const;
   uint32_t launches_per_step() const { return launches_; }
   PlanTuning& tuning() { return tune_; }
+  void set_tuning(const PlanTuning& t);
   size_t device_bytes() const { return dev_bytes_; }
   std::string last_error;
 
@@ -144,6 +148,8 @@ class Engine {
 
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
+  cudaStream_t aux_[2] = {nullptr, nullptr};  // graph branches (circles/polygons)
+  std::vector<struct CUevent_st*> evpool_;
   PlanTuning tune_;
   SchedRegistry reg_;
   std::vector<Slot> slots_;

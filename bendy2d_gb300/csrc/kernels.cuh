@@ -152,6 +152,27 @@ constexpr uint32_t STREAM_BYTES = 2 * SCHED_CHUNK_WORDS * 4 + 32;
 // positions (and prev) and links in shared memory too; !SMEM runs the same
 // schedule on global memory (bodies too large for one CTA).
 // ----------------------------------------------------------------------------
+// explicit shared-memory accesses on 32-bit shared addresses (so the body
+// state never goes through the generic load path)
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint2 lds_u32x2(uint32_t a) {
+  uint2 v;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float2 lds_f32x2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts_f32x2(uint32_t a, float2 v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+
 template <bool FULL, bool SMEM>
 __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
@@ -186,72 +207,27 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     if (S.nchunks > 0)
       bulk_load(cbuf, SC.stream + SC.chunk_off[S.chunk0], SC.chunk_len[S.chunk0] * 4u, &bar[0]);
   }
-
-  float2* sp = nullptr;
-  float2* sq = nullptr;
-  uint32_t* sab = nullptr;
-  float* srest = nullptr;
-  float* sstiff = nullptr;
+  // body state in shared memory: pos[np], prev[np] (FULL), {rest, stiff}[nl]
+  const uint32_t sp_a = smem_addr(base);
+  const uint32_t sq_a = sp_a + 8u * B.np;
+  const uint32_t srs_a = sq_a + (FULL ? 8u * B.np : 0u);
   if (SMEM) {
-    sp = reinterpret_cast<float2*>(base);
-    sq = sp + B.np;
-    sab = reinterpret_cast<uint32_t*>(sq + (FULL ? B.np : 0));
-    srest = reinterpret_cast<float*>(sab + B.nl);
-    sstiff = srest + B.nl;
     for (uint32_t i = t; i < B.np; i += T) {
       const uint32_t k = bidx[i];
-      sp[i] = gp[k];
-      if (FULL) sq[i] = gq[k];
+      sts_f32x2(sp_a + 8u * i, gp[k]);
+      if (FULL) sts_f32x2(sq_a + 8u * i, gq[k]);
     }
-    for (uint32_t i = t; i < B.nl; i += T) {
-      const uint2 ab = gab[i];
-      sab[i] = ab.x | (ab.y << 16);
-      srest[i] = grest[i];
-      sstiff[i] = gstiff[i];
-    }
+    for (uint32_t i = t; i < B.nl; i += T)
+      sts_f32x2(srs_a + 8u * i, make_float2(grest[i], gstiff[i]));
   }
   group_sync(g, T);
 
-  auto run = [&](uint32_t op) {
-    if (op & OP_INTEG) {
-      const uint32_t i = op & ~OP_INTEG;
-      float2* pp = SMEM ? sp + i : gp + bidx[i];
-      float2* qq = SMEM ? sq + i : gq + bidx[i];
-      float2 p = *pp, q = *qq;
-      solve_bounds(p, q, Wb);
-      integrate(p, q, gx, gy, h);
-      *pp = p;
-      *qq = q;
-    } else {
-      float2* pa;
-      float2* pb;
-      float rest, stiff;
-      if (SMEM) {
-        const uint32_t ab = sab[op];
-        pa = sp + (ab & 0xFFFFu);
-        pb = sp + (ab >> 16);
-        rest = srest[op];
-        stiff = sstiff[op];
-      } else {
-        const uint2 ab = gab[op];
-        pa = gp + ab.x;
-        pb = gp + ab.y;
-        rest = grest[op];
-        stiff = gstiff[op];
-      }
-      float2 a = *pa, b = *pb;
-      link_solve(a, b, rest, stiff);
-      *pa = a;
-      *pb = b;
-    }
-  };
-
+  const uint32_t cbuf_a = smem_addr(cbuf);
   // buffer k2 = c & 1 is used for the (c >> 1)-th time: its mbarrier phase
   // parity is (c >> 1) & 1
   for (uint32_t c = 0; c < S.nchunks; ++c) {
     const uint32_t k2 = c & 1u;
     const uint32_t par = (c >> 1) & 1u;
-    uint32_t* buf = cbuf + k2 * SCHED_CHUNK_WORDS;
     if (t == 0) *flag = mbar_wait_bounded(&bar[k2], par) ? 1u : 0u;
     group_sync(g, T);
     if (*flag == 0u) {
@@ -267,13 +243,56 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
       bulk_load(cbuf + (k2 ^ 1u) * SCHED_CHUNK_WORDS, SC.stream + SC.chunk_off[S.chunk0 + c + 1],
                 SC.chunk_len[S.chunk0 + c + 1] * 4u, &bar[k2 ^ 1u]);
     }
-    const uint32_t nseg = buf[0];
-    const uint32_t* ends = buf + 1;
-    const uint32_t* ops = buf + 1 + nseg;
+    const uint32_t buf_a = cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u;
+    const uint32_t nseg = lds_u32(buf_a);
+    const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
     uint32_t beg = 0;
     for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
-      const uint32_t end = ends[sgi];
-      for (uint32_t k = beg + t; k < end; k += T) run(ops[k]);
+      const uint32_t end = lds_u32(buf_a + 4u + 4u * sgi);
+      for (uint32_t k = beg + t; k < end; k += T) {
+        const uint2 op = lds_u32x2(ops_a + 8u * k);
+        if (op.y == OP_INTEG) {
+          float2 p, q;
+          if (SMEM) {
+            p = lds_f32x2(sp_a + 8u * op.x);
+            q = lds_f32x2(sq_a + 8u * op.x);
+          } else {
+            p = gp[bidx[op.x]];
+            q = gq[bidx[op.x]];
+          }
+          solve_bounds(p, q, Wb);
+          integrate(p, q, gx, gy, h);
+          if (SMEM) {
+            sts_f32x2(sp_a + 8u * op.x, p);
+            sts_f32x2(sq_a + 8u * op.x, q);
+          } else {
+            gp[bidx[op.x]] = p;
+            gq[bidx[op.x]] = q;
+          }
+        } else if (SMEM) {
+          const float2 rs = lds_f32x2(srs_a + 8u * op.y);
+          const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
+          float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
+          link_solve(pa, pb, rs.x, rs.y);
+          sts_f32x2(aa, pa);
+          sts_f32x2(ba, pb);
+        } else {
+          uint32_t ia, ib, kl;
+          if (op.y == OP_WIDE) {
+            kl = op.x;
+            ia = gab[kl].x;
+            ib = gab[kl].y;
+          } else {
+            kl = op.y;
+            ia = bidx[op.x & 0xFFFFu];
+            ib = bidx[op.x >> 16];
+          }
+          float2 pa = gp[ia], pb = gp[ib];
+          link_solve(pa, pb, grest[kl], gstiff[kl]);
+          gp[ia] = pa;
+          gp[ib] = pb;
+        }
+      }
       group_sync(g, T);
       beg = end;
     }
@@ -282,8 +301,8 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   if (SMEM) {
     for (uint32_t i = t; i < B.np; i += T) {
       const uint32_t k = bidx[i];
-      gp[k] = sp[i];
-      if (FULL) gq[k] = sq[i];
+      gp[k] = lds_f32x2(sp_a + 8u * i);
+      if (FULL) gq[k] = lds_f32x2(sq_a + 8u * i);
     }
   }
 }
@@ -911,7 +930,7 @@ __global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets)
   uint32_t run = s_off + block_exclusive_scan(v, nullptr);
 #pragma unroll
   for (uint32_t k = 0; k < 4; ++k) {
-    if (base + k < nbuckets) G.start[base + k] = run;
+    if (base + k < nbuckets) G.range[base + k] = make_uint2(run, c[k]);
     run += c[k];
   }
 }
@@ -928,7 +947,7 @@ __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __restrict
   const float2 p = W.pos[cur][j];
   const uint2 br = G.pbr[W.gp0 + j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell);
-  G.sorted[G.start[br.x] + br.y] =
+  G.sorted[G.range[br.x].x + br.y] =
       make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), j, (uint32_t)cx);
 }
 
@@ -1062,21 +1081,18 @@ __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __
                    b4 = B2D_BK(4), b5 = B2D_BK(5), b6 = B2D_BK(6), b7 = B2D_BK(7),
                    b8 = B2D_BK(8);
 #undef B2D_BK
-    const uint32_t n0 = G.count[b0], n1 = G.count[b1], n2 = G.count[b2], n3 = G.count[b3],
-                   n4 = G.count[b4], n5 = G.count[b5], n6 = G.count[b6], n7 = G.count[b7],
-                   n8 = G.count[b8];
-    const uint32_t s0 = G.start[b0], s1 = G.start[b1], s2 = G.start[b2], s3 = G.start[b3],
-                   s4 = G.start[b4], s5 = G.start[b5], s6 = G.start[b6], s7 = G.start[b7],
-                   s8 = G.start[b8];
-    visit_cell(G, W, i, p, cx - 1, cy - 1, s0, n0, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy - 1, s1, n1, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy - 1, s2, n2, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx - 1, cy, s3, n3, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy, s4, n4, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy, s5, n5, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx - 1, cy + 1, s6, n6, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy + 1, s7, n7, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy + 1, s8, n8, D, D2, sx, sy, hit);
+    const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2], r3 = G.range[b3],
+                r4 = G.range[b4], r5 = G.range[b5], r6 = G.range[b6], r7 = G.range[b7],
+                r8 = G.range[b8];
+    visit_cell(G, W, i, p, cx - 1, cy - 1, r0.x, r0.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy - 1, r1.x, r1.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy - 1, r2.x, r2.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx - 1, cy, r3.x, r3.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy, r4.x, r4.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy, r5.x, r5.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx - 1, cy + 1, r6.x, r6.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx, cy + 1, r7.x, r7.y, D, D2, sx, sy, hit);
+    visit_cell(G, W, i, p, cx + 1, cy + 1, r8.x, r8.y, D, D2, sx, sy, hit);
     if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
   }
   if (W.flags & COLLIDE_PC) p = particle_circles(W, p);

@@ -27,6 +27,21 @@ static uint32_t pow2ceil(uint32_t x) {
 }
 static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+bool PlanTuning::set(const std::string& k, double v) {
+  if (k == "serial_width") serial_width = (float)v;
+  else if (k == "t_min") t_min = (uint32_t)v;
+  else if (k == "t_max") t_max = (uint32_t)v;
+  else if (k == "pack_np") pack_np = (uint32_t)v;
+  else if (k == "pack_nl") pack_nl = (uint32_t)v;
+  else if (k == "free_chunk") free_chunk = (uint32_t)v;
+  else if (k == "smem_max") smem_max = (uint32_t)v;
+  else if (k == "warp_groups") warp_groups = (uint32_t)v;
+  else if (k == "max_groups") max_groups = (uint32_t)v;
+  else if (k == "width_per_thread") width_per_thread = (float)v;
+  else return false;
+  return true;
+}
+
 uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I,
                             bool full) {
   std::string key;
@@ -83,7 +98,8 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   d.chunk0 = (uint32_t)chunk_off.size();
   d.nlvl = maxl;
   d.nops = (uint32_t)total;
-  std::vector<uint32_t> seg_end, chunk_ops;
+  const bool narrow = np <= 65535u;
+  std::vector<uint32_t> seg_end, chunk_ops;  // chunk_ops: op ids
   auto flush = [&]() {
     if (seg_end.empty()) return;
     while (stream.size() % 4) stream.push_back(0);
@@ -91,7 +107,19 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
     const size_t at = stream.size();
     stream.push_back((uint32_t)seg_end.size());
     stream.insert(stream.end(), seg_end.begin(), seg_end.end());
-    stream.insert(stream.end(), chunk_ops.begin(), chunk_ops.end());
+    if ((stream.size() - at) % 2) stream.push_back(0);
+    for (uint32_t op : chunk_ops) {
+      if (op & OP_INTEG) {
+        stream.push_back(op & ~OP_INTEG);
+        stream.push_back(OP_INTEG);
+      } else if (narrow) {
+        stream.push_back(links[op].x | (links[op].y << 16));
+        stream.push_back(op);
+      } else {
+        stream.push_back(op);
+        stream.push_back(OP_WIDE);
+      }
+    }
     while ((stream.size() - at) % 4) stream.push_back(0);
     chunk_len.push_back((uint32_t)(stream.size() - at));
     if (chunk_len.back() > SCHED_CHUNK_WORDS) std::abort();
@@ -102,13 +130,14 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
     uint32_t b = start[l];
     const uint32_t e = start[l + 1];
     while (b < e) {
-      // words used: 1 (nseg) + segments + ops, plus 1 for this segment, padded to 4
-      size_t used = 1 + seg_end.size() + chunk_ops.size();
-      size_t room = SCHED_CHUNK_WORDS - 3 - used - 1;
-      if (used + 1 + 1 + 3 > SCHED_CHUNK_WORDS) {
+      // words: 1 (nseg) + segments (+1 for this one) + 1 pad + 2 per op + 3 pad
+      const size_t fixed = 1 + (seg_end.size() + 1) + 1 + 3;
+      const size_t used = fixed + 2 * chunk_ops.size();
+      if (used + 2 > SCHED_CHUNK_WORDS) {
         flush();
         continue;
       }
+      const size_t room = (SCHED_CHUNK_WORDS - used) / 2;
       const uint32_t take = (uint32_t)std::min<size_t>(room, e - b);
       chunk_ops.insert(chunk_ops.end(), sorted.begin() + b, sorted.begin() + b + take);
       seg_end.push_back((uint32_t)chunk_ops.size());
@@ -309,7 +338,7 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
     const float avg = S.nlvl ? (float)S.nops / (float)S.nlvl : 1.0f;
     uint32_t T = pow2ceil((uint32_t)(avg / tune.width_per_thread + 0.999f));
     T = std::min(std::max(T, tune.t_min), tune.t_max);
-    const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 12u * (size_t)B.nl);
+    const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 8u * (size_t)B.nl);
     const bool smem = region <= tune.smem_max && B.np <= 65535u;
     B.local = smem ? 1u : 0u;
     for (size_t i = 0; i < loc.size(); ++i) {

@@ -104,6 +104,10 @@ int b2d_set_link_iters(b2d_solver* s, uint32_t n);          /* apply_links repea
 int b2d_set_mode(b2d_solver* s, int mode);                  /* B2D_MODE_* */
 int b2d_set_collision(b2d_solver* s, uint32_t flags, float particle_radius, float grid_cell);
 int b2d_set_circle_static(b2d_solver* s, size_t index, int is_static);
+/* executor tunables (the autotuner sets these): serial_width, t_min, t_max,
+ * pack_np, pack_nl, free_chunk, smem_max, warp_groups, max_groups,
+ * width_per_thread; takes effect at the next update */
+int b2d_set_tuning(b2d_solver* s, const char* key, double value);
 
 int b2d_update(b2d_solver* s, float dt);                    /* Solver::update, :106-116 */
 
