@@ -41,6 +41,14 @@ class CCircle(C.Structure):
     _fields_ = [("point", CParticle), ("radius", C.c_float), ("is_static", C.c_uint32)]
 
 
+class CNoAllocParams(C.Structure):
+    _fields_ = [("gravity_x", C.c_float), ("gravity_y", C.c_float),
+                ("bounds_x", C.c_float), ("bounds_y", C.c_float),
+                ("bounds_w", C.c_float), ("bounds_h", C.c_float), ("dt", C.c_float),
+                ("sub_steps", C.c_uint32), ("particle_radius", C.c_float),
+                ("grid_cell", C.c_float)]
+
+
 class CPlanStats(C.Structure):
     _fields_ = [("bodies", C.c_uint32), ("group_bodies", C.c_uint32),
                 ("serial_bodies", C.c_uint32), ("global_bodies", C.c_uint32),
@@ -111,6 +119,7 @@ SIGNATURES = {
     "b2d_state_download_async": [_P, _P],
     "b2d_get_plan_stats": [_P, C.POINTER(CPlanStats)],
     "b2d_get_link_order": [_P, _U64, C.c_size_t],
+    "b2d_collide_substeps_noalloc": [_P, _P, C.c_size_t, C.POINTER(CNoAllocParams), _P],
     "b2d_batch_create": [C.POINTER(_P)],
     "b2d_batch_destroy": [_P],
     "b2d_batch_add": [_P, _P],

@@ -31,7 +31,7 @@ NVCC_FLAGS = [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              "-Wno-unused-function"]
 
-CU_SOURCES = ["engine.cu"]
+CU_SOURCES = ["engine.cu", "noalloc.cu"]
 CXX_SOURCES = ["host.cpp", "planner.cpp", "capi.cpp"]
 HEADERS = ["b2d_dev.h", "kernels.cuh", "engine.hpp", "host.hpp"]
 

@@ -23,6 +23,10 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+namespace b2d {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace b2d
+
 struct b2d_solver {
   WorldHost w;
   std::unique_ptr<Engine> own;

@@ -395,7 +395,7 @@ __device__ __forceinline__ float2 normalize2(float x, float y) {
 }
 
 // Polygon::resolve_line_intersection, src/polygon.rs:164-216
-__device__ bool resolve_line(float2 self_center, float2 pa, float2 pb, float2 q,
+static __device__ bool resolve_line(float2 self_center, float2 pa, float2 pb, float2 q,
                              float2 other_center, float2& na, float2& nb, float2& nq) {
   float2 I;
   if (!line_intersection(pa, pb, q, other_center, I)) return false;
@@ -854,7 +854,7 @@ constexpr uint32_t CHUNK = 256;  // particles per work chunk (one CTA)
 // Bucket entry: {pos.x bits, pos.y bits, particle index, cell x}.  An entry
 // belongs to cell (cx, cy) when its stored cell x equals cx and the cell y
 // recomputed from the stored pos.y equals cy: exact, whatever the hashing.
-__global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __restrict__ worlds, DGrid G,
+static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __restrict__ worlds, DGrid G,
                                                       const uint2* __restrict__ chunks,
                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
   if (blockIdx.x >= nchunks) return;
@@ -899,7 +899,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 }
 
 // sum of each SCAN_TILE counts
-__global__ void __launch_bounds__(1024) k_scan_reduce(DGrid G, uint32_t nbuckets) {
+static __global__ void __launch_bounds__(1024) k_scan_reduce(DGrid G, uint32_t nbuckets) {
   const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * 4u;
   uint32_t v = 0;
 #pragma unroll
@@ -911,7 +911,7 @@ __global__ void __launch_bounds__(1024) k_scan_reduce(DGrid G, uint32_t nbuckets
 }
 
 // start[b] = exclusive prefix sum of count (tile offset from the partials)
-__global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets) {
+static __global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets) {
   __shared__ uint32_t s_off;
   // offset of this tile: sum of the partials of the tiles before it
   uint32_t acc = 0;
@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets)
   }
 }
 
-__global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __restrict__ worlds, DGrid G,
+static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __restrict__ worlds, DGrid G,
                                                         const uint2* __restrict__ chunks,
                                                         uint32_t nchunks, uint32_t cur,
                                                         uint32_t sub) {
@@ -974,7 +974,7 @@ __device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D
 }
 
 // particle-Circle (circles are kinematic for particles; index order)
-__device__ float2 particle_circles(const DWorld& W, float2 p) {
+static __device__ float2 particle_circles(const DWorld& W, float2 p) {
   for (uint32_t k = 0; k < W.nc; ++k) {
     const float2 c = W.cpos[k];
     const float dx = fsub(p.x, c.x), dy = fsub(p.y, c.y);
@@ -992,7 +992,7 @@ __device__ float2 particle_circles(const DWorld& W, float2 p) {
 }
 
 // particle-Polygon edge projection (one-way)
-__device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p) {
+static __device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p) {
   const DPoly P = W.polys[k];
   if (P.nv < 3) return p;
   const float4 bb = W.paabb[k];
@@ -1057,7 +1057,7 @@ __device__ __forceinline__ void visit_cell(const DGrid& G, const DWorld& W, uint
 // Particle collisions + bounds + integrate of one sub-step of the extension
 // pipeline.  Reads positions from buffer cur (the post-link snapshot) and
 // writes the new ones to buffer cur^1; prev is updated in place.
-__global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __restrict__ worlds,
+static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __restrict__ worlds,
                                                              DGrid G, const uint2* __restrict__ chunks,
                                                              uint32_t nchunks, uint32_t cur,
                                                              uint32_t sub) {
@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __
 }
 
 // positions of worlds whose step ended in buffer 1 go back to buffer 0
-__global__ void __launch_bounds__(CHUNK) k_copy_back(const DWorld* __restrict__ worlds,
+static __global__ void __launch_bounds__(CHUNK) k_copy_back(const DWorld* __restrict__ worlds,
                                                      const uint2* __restrict__ chunks,
                                                      uint32_t nchunks) {
   if (blockIdx.x >= nchunks) return;

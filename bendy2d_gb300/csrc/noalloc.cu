@@ -1,0 +1,158 @@
+// noalloc.cu — b2d_collide_substeps_noalloc: particle-collision sub-steps on
+// caller-owned device arrays, with every byte of scratch memory in one
+// file-scope device array, so the call itself allocates nothing.
+//
+// Who needs it: callers that must not allocate GPU memory once they are
+// running — game and simulation frame loops that reserve all device memory
+// at start-up and forbid allocation per frame (cudaMalloc can synchronise
+// the device and stall the frame), and hosts that hand this library device
+// buffers they own and manage themselves.
+//
+// The scratch array (NOALLOC_BYTES, about 3.6 MB) stays resident on every GPU
+// that loads the library until the process exits.  Every call shares it and
+// it keeps the previous call's contents, so each call clears what must start
+// at zero; calls whose GPU work overlaps (different streams, or host threads
+// racing) corrupt each other.
+//
+// First call on a device: it resolves the array's device address with
+// cudaGetSymbolAddress while that device is current.  Make that first call
+// before capturing a CUDA stream into a graph.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/bendy2d.h"
+#include "kernels.cuh"
+
+namespace b2d {
+
+void set_last_error(const std::string& msg);  // capi.cpp: message for b2d_last_error()
+
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_PARTICLES = 65536;
+constexpr uint32_t NOALLOC_MAX_BUCKETS = 2 * NOALLOC_MAX_PARTICLES;  // power of two >= 2n
+constexpr uint32_t NOALLOC_MAX_CHUNKS = NOALLOC_MAX_PARTICLES / CHUNK;
+constexpr uint32_t NOALLOC_MAX_TILES = (NOALLOC_MAX_BUCKETS + SCAN_TILE - 1) / SCAN_TILE;
+
+constexpr size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+// layout of the scratch array
+constexpr size_t O_WORLD = 0;
+constexpr size_t O_CHUNKS = O_WORLD + up256(sizeof(DWorld));
+constexpr size_t O_COUNT = O_CHUNKS + up256(8 * NOALLOC_MAX_CHUNKS);
+constexpr size_t O_RANGE = O_COUNT + up256(4 * NOALLOC_MAX_BUCKETS);
+constexpr size_t O_PART = O_RANGE + up256(8 * NOALLOC_MAX_BUCKETS);
+constexpr size_t O_PBR = O_PART + up256(4 * NOALLOC_MAX_TILES);
+constexpr size_t O_SORTED = O_PBR + up256(8 * NOALLOC_MAX_PARTICLES);
+constexpr size_t O_POS1 = O_SORTED + up256(16 * NOALLOC_MAX_PARTICLES);
+constexpr size_t NOALLOC_BYTES = O_POS1 + up256(8 * NOALLOC_MAX_PARTICLES);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// device address of g_noalloc_scratch per device ordinal, resolved once
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+unsigned char* g_addr[kMaxDevices] = {};
+
+int fail(int code, const std::string& m) {
+  set_last_error(m);
+  return code;
+}
+
+// Writes the world record and the chunk list into the scratch array; the
+// parameters arrive as kernel arguments, so nothing is copied from the host.
+__global__ void k_noalloc_setup(DWorld w, uint2* chunks, uint32_t nchunks, DWorld* dst) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *dst = w;
+  if (i < nchunks) chunks[i] = make_uint2(0u, i * CHUNK);
+}
+
+}  // namespace
+
+}  // namespace b2d
+
+using namespace b2d;
+
+extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, size_t n,
+                                            const b2d_noalloc_params* p, void* cuda_stream) {
+  if (!p || (n && (!d_pos_xy || !d_prev_xy))) return fail(B2D_ERR_NULL, "null argument");
+  if (n > NOALLOC_MAX_PARTICLES)
+    return fail(B2D_ERR_CAPACITY, "b2d_collide_substeps_noalloc handles at most " +
+                                      std::to_string(NOALLOC_MAX_PARTICLES) + " particles, got " +
+                                      std::to_string(n));
+  if (!(p->particle_radius >= 0.0f && p->grid_cell > 0.0f &&
+        p->grid_cell >= 2.0f * p->particle_radius))
+    return fail(B2D_ERR_ARG, "needs radius >= 0 and grid cell >= 2 * radius");
+  if (n == 0 || p->sub_steps == 0) return B2D_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return fail(B2D_ERR_CUDA, "no current CUDA device");
+  unsigned char* base;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+      void* a = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+      if (e != cudaSuccess || !a)
+        return fail(B2D_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_addr[dev] = static_cast<unsigned char*>(a);
+    }
+    base = g_addr[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  const uint32_t np = (uint32_t)n;
+  uint32_t nb = 64;
+  while (nb < 2 * np) nb <<= 1;
+  const uint32_t nch = (np + CHUNK - 1) / CHUNK;
+  const uint32_t nt = (nb + SCAN_TILE - 1) / SCAN_TILE;
+
+  DWorld w;
+  std::memset(&w, 0, sizeof(w));
+  w.gx = 0.0f + p->gravity_x;  // acc = 0 + g at integrate time
+  w.gy = 0.0f + p->gravity_y;
+  w.bx = p->bounds_x;
+  w.by = p->bounds_y;
+  w.bw = p->bounds_w;
+  w.bh = p->bounds_h;
+  w.h = p->dt * (1.0f / (float)p->sub_steps);  // src/solver.rs:107-108
+  w.radius = p->particle_radius;
+  w.cell = p->grid_cell;
+  w.S = p->sub_steps;
+  w.I = 1;
+  w.flags = COLLIDE_PP;
+  w.np = np;
+  w.gb0 = 0;
+  w.gmask = nb - 1;
+  w.gp0 = 0;
+  w.pos[0] = reinterpret_cast<float2*>(d_pos_xy);
+  w.pos[1] = reinterpret_cast<float2*>(base + O_POS1);
+  w.prev = reinterpret_cast<float2*>(d_prev_xy);
+
+  DWorld* dW = reinterpret_cast<DWorld*>(base + O_WORLD);
+  uint2* chunks = reinterpret_cast<uint2*>(base + O_CHUNKS);
+  DGrid G;
+  G.count = reinterpret_cast<uint32_t*>(base + O_COUNT);
+  G.range = reinterpret_cast<uint2*>(base + O_RANGE);
+  G.partial = reinterpret_cast<uint32_t*>(base + O_PART);
+  G.pbr = reinterpret_cast<uint2*>(base + O_PBR);
+  G.sorted = reinterpret_cast<uint4*>(base + O_SORTED);
+  G.nbuckets = nb;
+
+  k_noalloc_setup<<<(nch + 255) / 256, 256, 0, st>>>(w, chunks, nch, dW);
+  for (uint32_t s = 0; s < w.S; ++s) {
+    const uint32_t cur = s & 1u;
+    if (cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st) != cudaSuccess)
+      return fail(B2D_ERR_CUDA, "clearing the bucket counts failed");
+    k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
+    k_scan_reduce<<<nt, 1024, 0, st>>>(G, nb);
+    k_scan_apply<<<nt, 1024, 0, st>>>(G, nb);
+    k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
+    k_collide_integrate<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
+  }
+  k_copy_back<<<nch, CHUNK, 0, st>>>(dW, chunks, nch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(B2D_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return B2D_OK;
+}

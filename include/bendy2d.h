@@ -159,6 +159,30 @@ int b2d_get_plan_stats(b2d_solver* s, b2d_plan_stats* out);
 /* fast mode: the link order actually executed (world link ids) */
 int b2d_get_link_order(b2d_solver* s, uint64_t* order, size_t cap);
 
+/* ---- particle-collision sub-steps without allocation ------------------- */
+/* No counterpart in the reference.  For callers that may not allocate GPU
+ * memory while running (frame loops that reserve all device memory at
+ * start-up, hosts that own and hand over every device buffer): runs
+ * `sub_steps` sub-steps of particle-particle collision (hashed grid,
+ * fixed-point Jacobi sum), bounds and Verlet integration on n link-free
+ * particles held in the caller's device arrays (pos/prev, x/y interleaved),
+ * in place, on `cuda_stream` -- the same arithmetic b2d_update applies to a
+ * solver holding only these particles with B2D_COLLIDE_PP.  Allocates
+ * nothing: all scratch lives in one static device array of about 3.6 MB
+ * (held by every GPU that loads the library until exit), so n is limited to
+ * 65536 (B2D_ERR_CAPACITY beyond).  Calls share that array: calls whose GPU
+ * work overlaps race.  The first call on a device resolves the array's
+ * address; make it before any stream capture. */
+typedef struct {
+  float gravity_x, gravity_y;
+  float bounds_x, bounds_y, bounds_w, bounds_h;
+  float dt;
+  uint32_t sub_steps;
+  float particle_radius, grid_cell;
+} b2d_noalloc_params;
+int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, size_t n,
+                                 const b2d_noalloc_params* params, void* cuda_stream);
+
 /* ---- batch: many independent solvers stepped by one launch sequence ---- */
 int b2d_batch_create(b2d_batch** out);
 int b2d_batch_destroy(b2d_batch* b);       /* members return to their own engines */
