@@ -137,6 +137,68 @@ def run_cpu_oracle(sc, budget_s: float, max_steps: int = 1000):
     return sc.n_particles * sc.sub_steps * steps / dt, steps, dt
 
 
+def run_batched_comparison(args, torch, flush, stream):
+    """Configuration 3: 4096 independent ring worlds (log-uniform 64..4096
+    particles) stepped (a) batched: one launch sequence for all worlds, CUDA
+    graph; (b) plain: one world per launch, no graph; (c) the CPU port of the
+    reference on a sample of worlds across all host cores."""
+    import concurrent.futures as cf
+    from bendy2d_gb300 import Batch, scenes
+    from oracle import load_scene
+    worlds = scenes.config3(seed=0, n_worlds=args.batched_worlds)
+    units = sum(w.n_particles * w.sub_steps for w in worlds)
+    dt = worlds[0].dt
+    out = {"workload": f"{len(worlds)} worlds of 1-8 hub-and-spoke rings, particles "
+                       "log-uniform in [64, 4096], 2 circles + floor polygon each, 8 sub-steps, "
+                       "1 link iteration", "worlds": len(worlds),
+           "particles": int(sum(w.n_particles for w in worlds))}
+
+    def timed_steps(batch, k):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                batch.update(dt)
+                e1.record(stream)
+        batch.synchronize()
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / k
+
+    b = Batch([w.to_solver() for w in worlds])
+    b.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        b.update(dt)
+    ms = timed_steps(b, args.batched_steps)
+    out["batched"] = {"value": units / (ms / 1e3), "ms_per_step": ms,
+                      "launches_per_step": b.launch_count()}
+    b.close()
+    p = Batch([w.to_solver() for w in worlds])
+    p.set_plain(True)
+    p.set_stream(stream.cuda_stream)
+    p.update(dt)
+    ms = timed_steps(p, max(1, min(3, args.batched_steps)))
+    out["plain"] = {"value": units / (ms / 1e3), "ms_per_step": ms,
+                    "launches_per_step": p.launch_count()}
+    p.close()
+    out["batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    # CPU port of the reference, worlds spread over all host cores
+    cores = os.cpu_count() or 1
+    sample = worlds[:: max(1, len(worlds) // args.cpu_worlds)][: args.cpu_worlds]
+    orcs = [load_scene(w) for w in sample]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(lambda o: o.update(dt), orcs))
+    el = time.perf_counter() - t0
+    su = sum(w.n_particles * w.sub_steps for w in sample)
+    out["cpu"] = {"value": su / el, "cores": cores, "kind": "port",
+                  "sample": f"{len(sample)} of the worlds, one update each, worlds across "
+                            f"{cores} threads"}
+    return out
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -152,6 +214,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-worlds", type=int, default=4096)
+    ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--cpu-worlds", type=int, default=512)
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -295,6 +361,10 @@ def main():
                "sample": f"{k} updates of the full workload in {el:.1f} s (C port of the "
                          "reference, single thread)"}
 
+    batched = None
+    if not args.no_batched and world == 1:
+        batched = run_batched_comparison(args, torch, flush, stream)
+
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
@@ -315,6 +385,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "batched_config3": batched,
     }
     print(json.dumps(out))
     if world > 1:

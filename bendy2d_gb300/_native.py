@@ -130,6 +130,7 @@ SIGNATURES = {
     "b2d_batch_set_profiling": [_P, C.c_int],
     "b2d_batch_get_profile": [_P, C.c_char_p, C.c_size_t, _F, C.c_size_t, _SZ],
     "b2d_batch_get_launch_count": [_P, C.POINTER(C.c_uint32)],
+    "b2d_batch_set_plain": [_P, C.c_int],
 }
 
 _lib = None

@@ -49,6 +49,7 @@ struct b2d_batch {
   std::vector<b2d_solver*> members;
   cudaStream_t stream = nullptr;
   bool profiling = false;
+  bool plain = false;
 };
 
 static int have_gpu() {
@@ -62,6 +63,7 @@ static int engine_for(b2d_solver* s, Engine** out) {
     if (!s->batch->eng) {
       if (!have_gpu()) return fail(ERR_CUDA, "no CUDA device: bendy2d-gb300 has no CPU path");
       s->batch->eng = std::make_unique<Engine>(s->batch->stream);
+      s->batch->eng->set_plain(s->batch->plain);
     }
     *out = s->batch->eng.get();
     return OK;
@@ -685,6 +687,12 @@ int b2d_batch_get_profile(b2d_batch* b, char* names, size_t names_cap, float* ms
                           size_t* count) {
   if (!b) return fail(ERR_NULL, "null batch");
   return put_profile(b->eng.get(), names, names_cap, ms, cap, count);
+}
+int b2d_batch_set_plain(b2d_batch* b, int on) {
+  if (!b) return fail(ERR_NULL, "null batch");
+  b->plain = on != 0;
+  if (b->eng) b->eng->set_plain(b->plain);
+  return OK;
 }
 int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out) {
   if (!b) return fail(ERR_NULL, "null batch");

@@ -40,6 +40,8 @@ static uint32_t pow2ceil_u(uint32_t x) {
 static int g_smem_optin = -1;
 static int g_num_sms = 0;
 static constexpr uint64_t kRigidSmemCap = 96 * 1024;
+static constexpr uint32_t kSerialPackBytes = 96 * 1024;  // shared memory per serial pack
+static constexpr uint32_t kSerialPackThreads = 64;       // bodies per serial pack
 
 Engine::Engine(cudaStream_t stream) : stream_(stream) {
   if (!stream_) {
@@ -57,6 +59,8 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     for (auto fn : {k_rigid<0>, k_rigid<1>, k_rigid<2>, k_rigid<3>})
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRigidSmemCap);
+    for (auto fn : {k_exec_serial_smem<true>, k_exec_serial_smem<false>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSerialPackBytes);
     cudaFuncSetAttribute(k_exec_groups<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
     cudaFuncSetAttribute(k_exec_groups<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
     cudaFuncSetAttribute(k_exec_groups<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
@@ -349,10 +353,55 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   return OK;
 }
 
+// First-fit decreasing: bodies sorted by size, each into the first pack with
+// room (bytes and threads).  Bodies larger than a pack stay in `rest` for the
+// global-memory serial kernel.
+void Engine::build_packs(std::vector<uint2>& in, bool full, SerialPacks& out,
+                         std::vector<uint2>& rest) {
+  const uint32_t per = full ? 16u : 8u;
+  auto np_of = [&](const uint2& it) { return slots_[it.x].img.bodies[it.y].np; };
+  std::stable_sort(in.begin(), in.end(),
+                   [&](const uint2& a, const uint2& b) { return np_of(a) > np_of(b); });
+  std::vector<std::vector<uint2>> bins;
+  std::vector<uint32_t> used;
+  size_t first_open = 0;
+  for (const uint2& it : in) {
+    const uint32_t bytes = np_of(it) * per;
+    if (bytes > kSerialPackBytes) {
+      rest.push_back(it);
+      continue;
+    }
+    size_t k = first_open;
+    while (k < bins.size() && (used[k] + bytes > kSerialPackBytes ||
+                               bins[k].size() >= kSerialPackThreads))
+      ++k;
+    if (k == bins.size()) {
+      bins.emplace_back();
+      used.push_back(0);
+    }
+    bins[k].push_back(it);
+    used[k] += bytes;
+    while (first_open < bins.size() && bins[first_open].size() >= kSerialPackThreads) ++first_open;
+  }
+  for (size_t k = 0; k < bins.size(); ++k) {
+    out.packs.push_back(make_uint2((uint32_t)out.items.size(), (uint32_t)bins[k].size()));
+    uint32_t base = 0;
+    for (const uint2& it : bins[k]) {
+      out.items.push_back(it);
+      out.sbase.push_back(base);
+      base += np_of(it);
+    }
+    out.max_bytes = std::max(out.max_bytes, base * per);
+  }
+}
+
 int Engine::rebuild_lists() {
   classes_.clear();
   serial_full_.clear();
   serial_links_.clear();
+  packs_full_ = SerialPacks();
+  packs_links_ = SerialPacks();
+  std::vector<uint2> sfull_all, slinks_all;
   chunks_.clear();
   rigid_full_.clear();
   rigid_ext_.clear();
@@ -362,11 +411,16 @@ int Engine::rebuild_lists() {
   size_t nbuckets = 0, np_pp = 0;
   uint64_t rigid_smem = 0;
   std::map<std::tuple<uint32_t, bool, bool, uint32_t>, size_t> cls;
+  wlaunch_.assign(slots_.size(), WorldLaunch());
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
     if (!s.live) continue;
     const WorldImage& im = s.img;
     const bool full = !im.ext;
+    std::vector<size_t> cls_before(classes_.size());
+    for (size_t c = 0; c < classes_.size(); ++c) cls_before[c] = classes_[c].items.size();
+    wlaunch_[si].sf0 = (uint32_t)serial_full_.size();
+    wlaunch_[si].pk0 = (uint32_t)packs_full_.packs.size();
     for (const GroupBody& gb : im.groups) {
       const uint32_t rc = gb.smem ? (gb.region + 4095u) & ~4095u : 0u;
       auto key = std::make_tuple(gb.T, gb.smem, full, rc);
@@ -388,7 +442,23 @@ int Engine::rebuild_lists() {
       }
       classes_[it->second].items.push_back(make_uint2(si, gb.body));
     }
-    for (uint32_t b : im.serials) (full ? serial_full_ : serial_links_).push_back(make_uint2(si, b));
+    if (plain_ && full) {  // plain mode: this world's own packs
+      std::vector<uint2> mine;
+      for (uint32_t b : im.serials) mine.push_back(make_uint2(si, b));
+      build_packs(mine, true, packs_full_, serial_full_);
+    } else {
+      for (uint32_t b : im.serials) (full ? sfull_all : slinks_all).push_back(make_uint2(si, b));
+    }
+    wlaunch_[si].sfn = (uint32_t)serial_full_.size() - wlaunch_[si].sf0;
+    wlaunch_[si].pkn = (uint32_t)packs_full_.packs.size() - wlaunch_[si].pk0;
+    for (size_t c = 0; c < classes_.size(); ++c) {
+      const size_t before = c < cls_before.size() ? cls_before[c] : 0;
+      if (classes_[c].items.size() > before)
+        wlaunch_[si].cls.emplace_back((uint32_t)before,
+                                      (uint32_t)(classes_[c].items.size() - before));
+      else
+        wlaunch_[si].cls.emplace_back(0u, 0u);
+    }
     const bool rigid = im.params.nc > 0 || im.params.ng > 0;
     if (rigid) {
       const uint64_t ng = im.polys.size(), nc = im.cpos.size(), nv = im.vpos.size();
@@ -398,7 +468,10 @@ int Engine::rebuild_lists() {
       if (need <= kRigidSmemCap) rigid_smem = std::max<uint64_t>(rigid_smem, need);
     }
     if (full) {
-      if (rigid) rigid_full_.push_back(si);
+      if (rigid) {
+        wlaunch_[si].rigid = (int32_t)rigid_full_.size();
+        rigid_full_.push_back(si);
+      }
     } else {
       if (rigid) rigid_ext_.push_back(si);
       smax_ext_ = std::max(smax_ext_, im.params.S);
@@ -421,13 +494,16 @@ int Engine::rebuild_lists() {
       np_ext += im.params.np;
     }
   }
+  if (!plain_) build_packs(sfull_all, true, packs_full_, serial_full_);
+  build_packs(slinks_all, false, packs_links_, serial_links_);
   // sort serial items longest first (load balance)
   auto serial_cost = [&](const uint2& a) {
     const DBody& B = slots_[a.x].img.bodies[a.y];
     return (uint64_t)B.nl * slots_[a.x].img.params.I + B.np;
   };
-  std::stable_sort(serial_full_.begin(), serial_full_.end(),
-                   [&](const uint2& a, const uint2& b) { return serial_cost(a) > serial_cost(b); });
+  if (!plain_)  // plain mode keeps each world's serial bodies contiguous
+    std::stable_sort(serial_full_.begin(), serial_full_.end(),
+                     [&](const uint2& a, const uint2& b) { return serial_cost(a) > serial_cost(b); });
   std::stable_sort(serial_links_.begin(), serial_links_.end(),
                    [&](const uint2& a, const uint2& b) { return serial_cost(a) > serial_cost(b); });
   // upload lists
@@ -442,9 +518,19 @@ int Engine::rebuild_lists() {
   all.insert(all.end(), serial_links_.begin(), serial_links_.end());
   off_chunks_ = all.size();
   all.insert(all.end(), chunks_.begin(), chunks_.end());
+  for (SerialPacks* sp : {&packs_full_, &packs_links_}) {
+    sp->off_items = all.size();
+    all.insert(all.end(), sp->items.begin(), sp->items.end());
+    sp->off_packs = all.size();
+    all.insert(all.end(), sp->packs.begin(), sp->packs.end());
+  }
   std::vector<uint32_t> wl(rigid_full_);
   off_rigid_ext_ = wl.size();
   wl.insert(wl.end(), rigid_ext_.begin(), rigid_ext_.end());
+  for (SerialPacks* sp : {&packs_full_, &packs_links_}) {
+    sp->off_sbase = wl.size();
+    wl.insert(wl.end(), sp->sbase.begin(), sp->sbase.end());
+  }
   if (all.size() > lists_cap_) {
     B2D_CUDA(cudaStreamSynchronize(stream_));
     cudaFree(d_lists_);
@@ -530,8 +616,54 @@ int Engine::launch_all(bool profiling) {
   };
   edge(stream_, ax);
   edge(stream_, ax2);
+  if (plain_) {
+    // one world at a time, each with its own launches
+    for (uint32_t si = 0; si < wlaunch_.size(); ++si) {
+      const WorldLaunch& wl = wlaunch_[si];
+      if (si >= slots_.size() || !slots_[si].live || slots_[si].img.ext) continue;
+      for (size_t c = 0; c < classes_.size() && c < wl.cls.size(); ++c) {
+        const LaunchClass& lc = classes_[c];
+        const uint32_t n = wl.cls[c].second;
+        if (!n || !lc.full) continue;
+        const dim3 grid((n + lc.G - 1) / lc.G), block(lc.T * lc.G);
+        const size_t sm = (size_t)lc.G * (lc.region + STREAM_BYTES);
+        const uint2* L = d_lists_ + lc.dev_off + wl.cls[c].first;
+        timed("plain_exec_groups", [&] {
+          if (lc.smem) k_exec_groups<true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, lc.T, lc.G, lc.region, 0, 0);
+          else k_exec_groups<true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, lc.T, lc.G, 0, 0, 0);
+        });
+      }
+      if (wl.pkn) {
+        const SerialPacks& P = packs_full_;
+        timed("plain_exec_serial_smem", [&] {
+          k_exec_serial_smem<true><<<wl.pkn, kSerialPackThreads, P.max_bytes, stream_>>>(
+              W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs + wl.pk0,
+              wl.pkn, 0, 0);
+        });
+      }
+      if (wl.sfn) {
+        timed("plain_exec_serial", [&] {
+          k_exec_serial<true><<<(wl.sfn + 127) / 128, 128, 0, stream_>>>(
+              W, d_lists_ + off_serial_full_ + wl.sf0, wl.sfn, 0, 0);
+        });
+      }
+      if (wl.rigid >= 0) {
+        timed("plain_rigid", [&] {
+          k_rigid<0><<<1, 128, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
+        });
+      }
+    }
+  } else {
   // worlds without extension collisions: one launch per class for the whole step
   groups(true, 0, 0);
+  if (!packs_full_.packs.empty()) {
+    const SerialPacks& P = packs_full_;
+    const uint32_t n = (uint32_t)P.packs.size();
+    timed("exec_serial_smem_full", [&] {
+      k_exec_serial_smem<true><<<n, kSerialPackThreads, P.max_bytes, stream_>>>(
+          W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, 0, 0);
+    });
+  }
   if (!serial_full_.empty()) {
     const uint32_t n = (uint32_t)serial_full_.size();
     timed("exec_serial_full", [&] {
@@ -541,6 +673,7 @@ int Engine::launch_all(bool profiling) {
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
     timed("rigid_full", [&] { k_rigid<0><<<n, 128, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
+  }
   }
   // worlds with extension collisions: per sub-step pipeline
   const uint32_t nch = (uint32_t)chunks_.size();
@@ -556,6 +689,14 @@ int Engine::launch_all(bool profiling) {
       });
     }
     groups(false, cur, s);
+    if (!packs_links_.packs.empty()) {
+      const SerialPacks& P = packs_links_;
+      const uint32_t n = (uint32_t)P.packs.size();
+      timed("exec_serial_smem_links", [&] {
+        k_exec_serial_smem<false><<<n, kSerialPackThreads, P.max_bytes, stream_>>>(
+            W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, cur, s);
+      });
+    }
     if (!serial_links_.empty()) {
       const uint32_t n = (uint32_t)serial_links_.size();
       timed("exec_serial_links", [&] {
@@ -604,7 +745,7 @@ int Engine::step() {
   if (lists_dirty_ && (st = rebuild_lists()) != OK) return st;
   if ((st = upload_registry()) != OK) return st;
   if (profile_) return launch_all(true);
-  if (!use_graph_) return launch_all(false);
+  if (!use_graph_ || plain_) return launch_all(false);
   if (!graph_valid_) {
     cudaGraph_t g = nullptr;
     B2D_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));

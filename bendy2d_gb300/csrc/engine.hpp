@@ -120,6 +120,9 @@ class Engine {
   cudaStream_t stream() const { return stream_; }
   void set_use_graph(bool on) { use_graph_ = on; invalidate_graph(); }
   void set_profile(bool on) { profile_ = on; }
+  // plain mode: every world without extension collisions gets its own
+  // launches (no batching, no graph) — the one-world-per-launch baseline
+  void set_plain(bool on) { plain_ = on; lists_dirty_ = true; invalidate_graph(); }
   // per-kernel timings of the last profiled step (ms), keyed by kernel name
   const std::vector<std::pair<std::string, float>>& last_profile() const { return prof_; }
   const WorldImage* image(uint32_t slot) const;
@@ -178,6 +181,24 @@ class Engine {
   size_t wlists_cap_ = 0;
   size_t off_rigid_ext_ = 0;
   uint32_t smax_ext_ = 0;
+  bool plain_ = false;
+  struct WorldLaunch {  // this world's ranges in the lists (plain mode)
+    std::vector<std::pair<uint32_t, uint32_t>> cls;  // per class: (offset, count)
+    uint32_t sf0 = 0, sfn = 0;                        // serial_full_
+    uint32_t pk0 = 0, pkn = 0;                        // packs_full_.packs
+    int32_t rigid = -1;                               // index into rigid_full_
+  };
+  // chain-like bodies packed into shared-memory CTAs (k_exec_serial_smem)
+  struct SerialPacks {
+    std::vector<uint2> items;     // pack order
+    std::vector<uint32_t> sbase;  // first shared slot of each item
+    std::vector<uint2> packs;     // {first item, item count}
+    uint32_t max_bytes = 0;
+    size_t off_items = 0, off_packs = 0, off_sbase = 0;
+  };
+  SerialPacks packs_full_, packs_links_;
+  void build_packs(std::vector<uint2>& in, bool full, SerialPacks& out, std::vector<uint2>& rest);
+  std::vector<WorldLaunch> wlaunch_;
   bool any_pp_ = false;
   uint32_t rigid_smem_ = 0;
   uint32_t grid_used_ = 0;

@@ -246,55 +246,80 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     const uint32_t buf_a = cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u;
     const uint32_t nseg = lds_u32(buf_a);
     const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
-    uint32_t beg = 0;
-    for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
-      const uint32_t end = lds_u32(buf_a + 4u + 4u * sgi);
-      for (uint32_t k = beg + t; k < end; k += T) {
-        const uint2 op = lds_u32x2(ops_a + 8u * k);
-        if (op.y == OP_INTEG) {
-          float2 p, q;
-          if (SMEM) {
-            p = lds_f32x2(sp_a + 8u * op.x);
-            q = lds_f32x2(sq_a + 8u * op.x);
-          } else {
-            p = gp[bidx[op.x]];
-            q = gq[bidx[op.x]];
-          }
-          solve_bounds(p, q, Wb);
-          integrate(p, q, gx, gy, h);
-          if (SMEM) {
-            sts_f32x2(sp_a + 8u * op.x, p);
-            sts_f32x2(sq_a + 8u * op.x, q);
-          } else {
-            gp[bidx[op.x]] = p;
-            gq[bidx[op.x]] = q;
-          }
-        } else if (SMEM) {
-          const float2 rs = lds_f32x2(srs_a + 8u * op.y);
-          const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
-          float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
-          link_solve(pa, pb, rs.x, rs.y);
-          sts_f32x2(aa, pa);
-          sts_f32x2(ba, pb);
+    // The op stream is immutable: each thread fetches the next segment's end,
+    // its first op there and that link's {rest, stiffness} before the
+    // barrier, so after it only the position loads remain on the path.
+    auto fetch_op = [&](uint32_t k, uint32_t e) {
+      return k < e ? lds_u32x2(ops_a + 8u * k) : make_uint2(0u, OP_NONE);
+    };
+    auto fetch_rs = [&](uint2 op) {
+      return (SMEM && op.y < OP_INTEG) ? lds_f32x2(srs_a + 8u * op.y) : make_float2(0.f, 0.f);
+    };
+    auto run = [&](uint2 op, float2 rs) {
+      if (op.y == OP_NONE) return;
+      if (op.y == OP_INTEG) {
+        float2 p, q;
+        if (SMEM) {
+          p = lds_f32x2(sp_a + 8u * op.x);
+          q = lds_f32x2(sq_a + 8u * op.x);
         } else {
-          uint32_t ia, ib, kl;
-          if (op.y == OP_WIDE) {
-            kl = op.x;
-            ia = gab[kl].x;
-            ib = gab[kl].y;
-          } else {
-            kl = op.y;
-            ia = bidx[op.x & 0xFFFFu];
-            ib = bidx[op.x >> 16];
-          }
-          float2 pa = gp[ia], pb = gp[ib];
-          link_solve(pa, pb, grest[kl], gstiff[kl]);
-          gp[ia] = pa;
-          gp[ib] = pb;
+          p = gp[bidx[op.x]];
+          q = gq[bidx[op.x]];
         }
+        solve_bounds(p, q, Wb);
+        integrate(p, q, gx, gy, h);
+        if (SMEM) {
+          sts_f32x2(sp_a + 8u * op.x, p);
+          sts_f32x2(sq_a + 8u * op.x, q);
+        } else {
+          gp[bidx[op.x]] = p;
+          gq[bidx[op.x]] = q;
+        }
+      } else if (SMEM) {
+        const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
+        float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
+        link_solve(pa, pb, rs.x, rs.y);
+        sts_f32x2(aa, pa);
+        sts_f32x2(ba, pb);
+      } else {
+        uint32_t ia, ib, kl;
+        if (op.y == OP_WIDE) {
+          kl = op.x;
+          ia = gab[kl].x;
+          ib = gab[kl].y;
+        } else {
+          kl = op.y;
+          ia = bidx[op.x & 0xFFFFu];
+          ib = bidx[op.x >> 16];
+        }
+        float2 pa = gp[ia], pb = gp[ib];
+        link_solve(pa, pb, grest[kl], gstiff[kl]);
+        gp[ia] = pa;
+        gp[ib] = pb;
       }
+    };
+    uint32_t beg = 0;
+    uint32_t end = lds_u32(buf_a + 4u);
+    uint2 op = fetch_op(t, end);
+    float2 rs = fetch_rs(op);
+    for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
+      uint32_t end_n = end;
+      uint2 op_n = make_uint2(0u, OP_NONE);
+      if (sgi + 1 < nseg) {
+        end_n = lds_u32(buf_a + 8u + 4u * sgi);
+        op_n = fetch_op(end + t, end_n);
+      }
+      run(op, rs);
+      for (uint32_t k = beg + t + T; k < end; k += T) {
+        const uint2 o2 = lds_u32x2(ops_a + 8u * k);
+        run(o2, fetch_rs(o2));
+      }
+      const float2 rs_n = fetch_rs(op_n);
       group_sync(g, T);
       beg = end;
+      end = end_n;
+      op = op_n;
+      rs = rs_n;
     }
   }
 
@@ -311,7 +336,8 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 // Serial executor: one thread replays one body's reference loops directly, in
 // insertion order (src/solver.rs:143-146, :155-158, :118-121).  Used for
 // chain-like bodies (rings, ropes) whose level schedule has width ~1, where a
-// whole group would idle.  Link endpoints are world indices.
+// whole group would idle.  This variant works on global memory (bodies too
+// large for a shared-memory pack).
 // ----------------------------------------------------------------------------
 template <bool FULL>
 __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __restrict__ list,
@@ -335,11 +361,12 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
   for (uint32_t s = 0; s < nsub; ++s) {
     for (uint32_t it = 0; it < I; ++it) {
       for (uint32_t k = 0; k < B.nl; ++k) {
-        const uint2 e = ab[k];
-        float2 pa = p[e.x], pb = p[e.y];
+        const uint2 e = ab[k];  // body-local endpoints
+        const uint32_t ia = bidx[e.x], ib = bidx[e.y];
+        float2 pa = p[ia], pb = p[ib];
         link_solve(pa, pb, rest[k], stiff[k]);
-        p[e.x] = pa;
-        p[e.y] = pb;
+        p[ia] = pa;
+        p[ib] = pb;
       }
     }
     if (FULL) {
@@ -351,6 +378,95 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
         p[j] = pp;
         q[j] = qq;
       }
+    }
+  }
+}
+
+// Serial executor, shared-memory variant: a CTA runs a pack of chain-like
+// bodies, one thread per body, with every body's positions (and prev) staged
+// in shared memory, so each link of the chain costs shared-memory latency
+// instead of a global round trip.  pack = {first item, item count}; sbase[i]
+// is item i's first particle slot in the pack's shared array.
+template <bool FULL>
+__global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
+                                   const uint2* __restrict__ items,
+                                   const uint32_t* __restrict__ sbase,
+                                   const uint2* __restrict__ packs, uint32_t npacks, uint32_t cur,
+                                   uint32_t sub) {
+  extern __shared__ __align__(16) float2 sstate[];
+  if (blockIdx.x >= npacks) return;
+  const uint2 pk = packs[blockIdx.x];
+  const uint32_t tid = threadIdx.x, nt = blockDim.x;
+  const uint32_t warp = tid >> 5, lane = tid & 31u, nwarps = nt >> 5;
+  // pack-wide particle count -> prev slots follow the pos slots
+  const uint32_t last = pk.x + pk.y - 1;
+  const uint32_t total = sbase[last] + worlds[items[last].x].bodies[items[last].y].np;
+  float2* spos = sstate;
+  float2* sprev = sstate + total;
+  // cooperative load, one warp per body
+  for (uint32_t it = warp; it < pk.y; it += nwarps) {
+    const uint2 wi = items[pk.x + it];
+    const DWorld& W = worlds[wi.x];
+    if (!FULL && sub >= W.S) continue;
+    const DBody B = W.bodies[wi.y];
+    const uint32_t* bidx = W.bidx + B.i0;
+    const uint32_t sb = sbase[pk.x + it];
+    for (uint32_t i = lane; i < B.np; i += 32) {
+      const uint32_t k = bidx[i];
+      spos[sb + i] = W.pos[cur][k];
+      if (FULL) sprev[sb + i] = W.prev[k];
+    }
+  }
+  __syncthreads();
+  if (tid < pk.y) {
+    const uint2 wi = items[pk.x + tid];
+    const DWorld& W = worlds[wi.x];
+    if (FULL || sub < W.S) {
+      const DBody B = W.bodies[wi.y];
+      const uint32_t sb = sbase[pk.x + tid];
+      float2* p = spos + sb;
+      float2* q = sprev + sb;
+      const uint2* ab = W.lab + B.l0;  // body-local endpoints
+      const float* rest = W.lrest + B.l0;
+      const float* stiff = W.lstiff + B.l0;
+      const uint32_t nsub = FULL ? W.S : 1u, I = W.I;
+      const float gx = W.gx, gy = W.gy, h = W.h;
+      DWorld Wb;
+      Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+      for (uint32_t s = 0; s < nsub; ++s) {
+        for (uint32_t it = 0; it < I; ++it) {
+          for (uint32_t k = 0; k < B.nl; ++k) {
+            const uint2 e = __ldg(ab + k);
+            float2 pa = p[e.x], pb = p[e.y];
+            link_solve(pa, pb, __ldg(rest + k), __ldg(stiff + k));
+            p[e.x] = pa;
+            p[e.y] = pb;
+          }
+        }
+        if (FULL) {
+          for (uint32_t k = 0; k < B.np; ++k) {
+            float2 pp = p[k], qq = q[k];
+            solve_bounds(pp, qq, Wb);
+            integrate(pp, qq, gx, gy, h);
+            p[k] = pp;
+            q[k] = qq;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t it = warp; it < pk.y; it += nwarps) {
+    const uint2 wi = items[pk.x + it];
+    const DWorld& W = worlds[wi.x];
+    if (!FULL && sub >= W.S) continue;
+    const DBody B = W.bodies[wi.y];
+    const uint32_t* bidx = W.bidx + B.i0;
+    const uint32_t sb = sbase[pk.x + it];
+    for (uint32_t i = lane; i < B.np; i += 32) {
+      const uint32_t k = bidx[i];
+      W.pos[cur][k] = spos[sb + i];
+      if (FULL) W.prev[k] = sprev[sb + i];
     }
   }
 }

@@ -172,7 +172,6 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
     for (uint32_t i = 0; i < B.np; ++i)
       if (im.bidx[B.i0 + i] >= P.np) return bad("body particle index");
     const uint32_t lim = B.local ? B.np : P.np;
-    if (B.local && B.np > 65535u) return bad("local body too large");
     for (uint32_t k = 0; k < B.nl; ++k) {
       const uint2 e = im.lab[B.l0 + k];
       if (e.x >= lim || e.y >= lim || e.x == e.y) return bad("link endpoint");
@@ -184,11 +183,11 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
     if (B.sched >= reg.scheds.size()) return bad("schedule id");
     const DSched& S = reg.scheds[B.sched];
     if ((size_t)S.chunk0 + S.nchunks > reg.chunk_off.size()) return bad("schedule range");
-    if (g.smem && !B.local) return bad("shared-memory body without local links");
+    if (g.smem && (!B.local || B.np > 65535u)) return bad("shared-memory body needs local links");
     if (g.T < 32 || g.T % 32) return bad("group size");
   }
   for (uint32_t b : im.serials)
-    if (b >= im.bodies.size() || im.bodies[b].local) return bad("serial body");
+    if (b >= im.bodies.size() || !im.bodies[b].local) return bad("serial body");
   if (im.cpos.size() != P.nc || im.crad.size() != P.nc) return bad("circle arrays");
   for (const uint2& e : im.clab)
     if (e.x >= P.nc || e.y >= P.nc) return bad("circle link");
@@ -372,11 +371,15 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
       B.np = (uint32_t)c.parts.size();
       B.l0 = (uint32_t)im.lab.size();
       B.nl = (uint32_t)c.links.size();
-      B.local = 0;
-      for (uint32_t p : c.parts) im.bidx.push_back(p);
+      B.local = 1;  // body-local endpoints: index into the body's particle list
+      uint32_t nloc = 0;
+      for (uint32_t p : c.parts) {
+        local[p] = nloc++;
+        im.bidx.push_back(p);
+      }
       for (uint32_t k : c.links) {
         const Link& L = w.particle_links[k];
-        im.lab.push_back(make_uint2((uint32_t)L.particle_a, (uint32_t)L.particle_b));
+        im.lab.push_back(make_uint2(local[L.particle_a], local[L.particle_b]));
         im.lrest.push_back(L.target_distance);
         im.lstiff.push_back(L.stiffness);
       }

@@ -195,6 +195,9 @@ int b2d_batch_set_profiling(b2d_batch* b, int on);
 int b2d_batch_get_profile(b2d_batch* b, char* names, size_t names_cap, float* ms, size_t cap,
                           size_t* count);
 int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out);
+/* plain mode: each member world gets its own launches (no batching, no CUDA
+ * graph) — the one-world-per-launch baseline the batched path is compared to */
+int b2d_batch_set_plain(b2d_batch* b, int on);
 
 #ifdef __cplusplus
 }

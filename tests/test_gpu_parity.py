@@ -252,6 +252,26 @@ def test_batch_equals_alone(gpu):
     b.close()
 
 
+def test_plain_mode_equals_batched(gpu):
+    """The one-world-per-launch baseline computes the same bits."""
+    from bendy2d_gb300 import Batch, scenes
+    rng = np.random.default_rng(31)
+    worlds = [scenes.config3_world(rng, int(n)) for n in rng.integers(64, 900, size=8)]
+    worlds.append(scenes.config1(seed=4))
+    a = [w.to_solver() for w in worlds]
+    b = [w.to_solver() for w in worlds]
+    ba, bb = Batch(a), Batch(b)
+    bb.set_plain(True)
+    for _ in range(3):
+        ba.update(worlds[0].dt)
+        bb.update(worlds[0].dt)
+    assert bb.launch_count() > ba.launch_count()
+    for x, y in zip(a, b):
+        assert_same_state(solver_state(x), solver_state(y), "plain vs batched")
+    ba.close()
+    bb.close()
+
+
 def test_write_state_roundtrip_and_clone(gpu):
     from bendy2d_gb300 import scenes
     sc = scenes.config1(seed=1)
