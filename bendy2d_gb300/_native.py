@@ -49,6 +49,12 @@ class CNoAllocParams(C.Structure):
                 ("grid_cell", C.c_float)]
 
 
+class CServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "admitted", "completed", "failed",
+                                          "queued", "active", "ticks", "particle_substeps",
+                                          "resident_bytes")]
+
+
 class CPlanStats(C.Structure):
     _fields_ = [("bodies", C.c_uint32), ("group_bodies", C.c_uint32),
                 ("serial_bodies", C.c_uint32), ("global_bodies", C.c_uint32),
@@ -131,6 +137,15 @@ SIGNATURES = {
     "b2d_batch_get_profile": [_P, C.c_char_p, C.c_size_t, _F, C.c_size_t, _SZ],
     "b2d_batch_get_launch_count": [_P, C.POINTER(C.c_uint32)],
     "b2d_batch_set_plain": [_P, C.c_int],
+    "b2d_server_create": [C.c_uint64, C.POINTER(_P)],
+    "b2d_server_destroy": [_P],
+    "b2d_server_start": [_P],
+    "b2d_server_stop": [_P],
+    "b2d_server_submit": [_P, _P, C.c_uint32, C.c_float, C.POINTER(C.c_uint64)],
+    "b2d_server_poll": [_P, C.c_uint64, C.POINTER(C.c_int)],
+    "b2d_server_take": [_P, C.c_uint64, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "b2d_server_get_stats": [_P, C.POINTER(CServerStats)],
+    "b2d_server_finished": [_P, C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_size_t)],
 }
 
 _lib = None

@@ -32,8 +32,8 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
              "-Wno-unused-function"]
 
 CU_SOURCES = ["engine.cu", "noalloc.cu"]
-CXX_SOURCES = ["host.cpp", "planner.cpp", "capi.cpp"]
-HEADERS = ["b2d_dev.h", "kernels.cuh", "engine.hpp", "host.hpp"]
+CXX_SOURCES = ["host.cpp", "planner.cpp", "capi.cpp", "server.cpp"]
+HEADERS = ["b2d_dev.h", "kernels.cuh", "engine.hpp", "host.hpp", "server.hpp"]
 
 
 def _nvcc() -> str:

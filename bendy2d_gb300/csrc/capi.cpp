@@ -13,6 +13,7 @@
 
 #include "../../include/bendy2d.h"
 #include "engine.hpp"
+#include "server.hpp"
 
 using namespace b2d;
 
@@ -42,6 +43,11 @@ struct b2d_solver {
   bool profiling = false;
   PlanTuning tune;
   bool tune_set = false;
+};
+
+struct b2d_server {
+  std::unique_ptr<Server> sv;
+  std::vector<uint64_t> pending;  // finished ids not yet handed out
 };
 
 struct b2d_batch {
@@ -697,6 +703,79 @@ int b2d_batch_set_plain(b2d_batch* b, int on) {
 int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out) {
   if (!b) return fail(ERR_NULL, "null batch");
   *out = b->eng ? b->eng->launches_per_step() : 0;
+  return OK;
+}
+
+// ---- serving ---------------------------------------------------------------
+int b2d_server_create(uint64_t budget_bytes, b2d_server** out) {
+  if (!out) return fail(ERR_NULL, "null out");
+  if (!have_gpu()) return fail(ERR_CUDA, "no CUDA device: bendy2d-gb300 has no CPU path");
+  *out = new b2d_server();
+  (*out)->sv = std::make_unique<Server>(budget_bytes);
+  return OK;
+}
+int b2d_server_destroy(b2d_server* sv) {
+  if (!sv) return OK;
+  sv->sv->stop();
+  delete sv;
+  return OK;
+}
+int b2d_server_start(b2d_server* sv) {
+  if (!sv) return fail(ERR_NULL, "null server");
+  return sv->sv->start();
+}
+int b2d_server_stop(b2d_server* sv) {
+  if (!sv) return fail(ERR_NULL, "null server");
+  return sv->sv->stop();
+}
+int b2d_server_submit(b2d_server* sv, b2d_solver* world, uint32_t steps, float dt, uint64_t* id) {
+  if (!sv || !world || !id) return fail(ERR_NULL, "null argument");
+  int st = sync_host(world);
+  if (st != OK) return st;
+  std::string why;
+  st = sv->sv->submit(world->w, steps, dt, id, &why);
+  return st == OK ? OK : fail(st, why);
+}
+int b2d_server_poll(b2d_server* sv, uint64_t id, int* state) {
+  if (!sv || !state) return fail(ERR_NULL, "null argument");
+  int st = sv->sv->poll(id, state);
+  return st == OK ? OK : fail(st, "unknown request id");
+}
+int b2d_server_take(b2d_server* sv, uint64_t id, b2d_solver* dst, double* latency_s,
+                    double* queue_s) {
+  if (!sv || !dst) return fail(ERR_NULL, "null argument");
+  int st = unplace(dst);
+  if (st != OK) return st;
+  std::string why;
+  st = sv->sv->take(id, &dst->w, latency_s, queue_s, &why);
+  if (st != OK) return fail(st, why);
+  dst->topo_dirty = true;
+  dst->host_stale = false;
+  return OK;
+}
+int b2d_server_finished(b2d_server* sv, uint64_t* ids, size_t cap, size_t* n) {
+  if (!sv || !n) return fail(ERR_NULL, "null argument");
+  std::vector<uint64_t>& pend = sv->pending;
+  std::vector<uint64_t> more = sv->sv->finished();
+  pend.insert(pend.end(), more.begin(), more.end());
+  const size_t k = std::min(cap, pend.size());
+  if (k && ids) std::memcpy(ids, pend.data(), k * sizeof(uint64_t));
+  pend.erase(pend.begin(), pend.begin() + k);
+  *n = k;
+  return OK;
+}
+int b2d_server_get_stats(b2d_server* sv, b2d_server_stats* out) {
+  if (!sv || !out) return fail(ERR_NULL, "null argument");
+  const ServerStats s = sv->sv->stats();
+  out->submitted = s.submitted;
+  out->admitted = s.admitted;
+  out->completed = s.completed;
+  out->failed = s.failed;
+  out->queued = s.queued;
+  out->active = s.active;
+  out->ticks = s.ticks;
+  out->particle_substeps = s.particle_substeps;
+  out->resident_bytes = s.resident_bytes;
   return OK;
 }
 

@@ -95,6 +95,7 @@ void Engine::invalidate_graph() {
     graph_ = nullptr;
   }
   graph_valid_ = false;
+  stable_steps_ = 0;
 }
 
 void Engine::set_stream(cudaStream_t s) {
@@ -746,6 +747,12 @@ int Engine::step() {
   if ((st = upload_registry()) != OK) return st;
   if (profile_) return launch_all(true);
   if (!use_graph_ || plain_) return launch_all(false);
+  // capture a graph once the composition has been stable for two steps;
+  // a batch that changes every step (serving) keeps launching eagerly
+  if (!graph_valid_ && stable_steps_ < 2) {
+    ++stable_steps_;
+    return launch_all(false);
+  }
   if (!graph_valid_) {
     cudaGraph_t g = nullptr;
     B2D_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));

@@ -212,6 +212,7 @@ class Engine {
   bool use_graph_ = true;
   cudaGraphExec_t graph_ = nullptr;
   bool graph_valid_ = false;
+  uint32_t stable_steps_ = 0;
   bool profile_ = false;
   std::vector<std::pair<std::string, float>> prof_;
   uint32_t launches_ = 0;

@@ -1,0 +1,240 @@
+// server.cpp — continuous-batching request loop for world-solve requests.
+//
+// A request is a world (a copy of a solver's contents) plus a number of
+// Solver::update calls.  A worker thread repeats one tick:
+//   1. admit queued requests, first come first served, while the device bytes
+//      of the resident worlds plus the candidate stay within the budget;
+//   2. one Solver::update for every resident world, all in one launch sequence
+//      of a shared Engine (the same batched kernels as b2d_batch_update);
+//   3. retire requests that reached their step count: copy the state back,
+//      free the world's device block, record the latency.
+// Requests that arrive while a tick runs wait in the queue and join at the
+// next tick, so work overlaps on the device as memory frees up.  World state
+// stays device-resident across ticks.  Every world is computed independently
+// (per-world grids, order-independent sums), so a result is bit-identical
+// whether the request ran alone or in a mix.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "engine.hpp"
+#include "server.hpp"
+
+namespace b2d {
+
+using Clock = std::chrono::steady_clock;
+
+struct Server::Req {
+  uint64_t id;
+  WorldHost world;
+  uint32_t steps = 0, done = 0;
+  float dt = 0.0f;
+  int state = SERVE_QUEUED;
+  uint32_t slot = 0;
+  size_t bytes = 0;
+  Clock::time_point t_submit, t_admit, t_done;
+  std::string error;
+};
+
+Server::Server(uint64_t budget) : budget_(budget) {}
+
+Server::~Server() { stop(); }
+
+int Server::start() {
+  std::lock_guard<std::mutex> lk(mu_);
+  if (running_) return OK;
+  running_ = true;
+  worker_ = std::thread([this] { loop(); });
+  return OK;
+}
+
+int Server::stop() {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (!running_) return OK;
+    running_ = false;
+  }
+  cv_.notify_all();
+  if (worker_.joinable()) worker_.join();
+  return OK;
+}
+
+// Upper bound of the device bytes a world holds while resident: its block
+// (every array at its largest: one body per particle) plus its share of the
+// collision grid.
+size_t Server::estimate_bytes(const WorldHost& w) {
+  const size_t np = w.particles.size(), nl = w.particle_links.size(), nc = w.circles.size(),
+               ng = w.polygons.size();
+  size_t nv = 0, npl = 0;
+  for (const Polygon& g : w.polygons) {
+    nv += g.particles.size();
+    npl += g.particle_links.size();
+  }
+  size_t b = 24 * np + 4 * np + sizeof(DBody) * np + 16 * nl;
+  b += 36 * nc + 12 * w.circle_links.size();
+  b += 24 * nv + (sizeof(DPoly) + 24) * ng + 12 * npl + 4 * (ng * ng + 1);
+  if (w.collide) b += 48 * np + 64;
+  return b + 32 * 16;
+}
+
+int Server::submit(const WorldHost& w, uint32_t steps, float dt, uint64_t* id, std::string* why) {
+  int st = validate_world(w, why);
+  if (st != OK) return st;
+  const size_t bytes = estimate_bytes(w);
+  if (bytes > budget_) {
+    if (why) *why = "world needs " + std::to_string(bytes) + " device bytes, budget is " +
+                    std::to_string(budget_);
+    return ERR_BUDGET;
+  }
+  auto r = std::make_unique<Req>();
+  r->world = w;
+  r->steps = steps;
+  r->dt = dt;
+  r->bytes = bytes;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    r->id = next_id_++;
+    *id = r->id;
+    queue_.push_back(r.get());
+    reqs_.emplace(r->id, std::move(r));
+    ++stats_.submitted;
+  }
+  cv_.notify_all();
+  return OK;
+}
+
+int Server::poll(uint64_t id, int* state) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = reqs_.find(id);
+  if (it == reqs_.end()) return ERR_INDEX;
+  *state = it->second->state;
+  return OK;
+}
+
+int Server::take(uint64_t id, WorldHost* out, double* latency_s, double* queue_s,
+                 std::string* why) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = reqs_.find(id);
+  if (it == reqs_.end()) return ERR_INDEX;
+  Req& r = *it->second;
+  if (r.state == SERVE_FAILED) {
+    if (why) *why = r.error;
+    reqs_.erase(it);
+    return ERR_STATE;
+  }
+  if (r.state != SERVE_DONE) {
+    if (why) *why = "request not finished";
+    return ERR_STATE;
+  }
+  if (out) *out = std::move(r.world);
+  if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+  if (queue_s) *queue_s = std::chrono::duration<double>(r.t_admit - r.t_submit).count();
+  reqs_.erase(it);
+  return OK;
+}
+
+std::vector<uint64_t> Server::finished() {
+  std::lock_guard<std::mutex> lk(mu_);
+  std::vector<uint64_t> out;
+  out.swap(finished_);
+  return out;
+}
+
+ServerStats Server::stats() {
+  std::lock_guard<std::mutex> lk(mu_);
+  ServerStats s = stats_;
+  s.queued = queue_.size();
+  s.active = active_.size();
+  s.resident_bytes = resident_;
+  return s;
+}
+
+void Server::loop() {
+  std::unique_ptr<Engine> eng;
+  for (;;) {
+    std::vector<Req*> admit;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_.wait(lk, [&] { return !running_ || !queue_.empty() || !active_.empty(); });
+      if (!running_) break;
+      // first come, first served while the budget holds
+      while (!queue_.empty() && resident_ + queue_.front()->bytes <= budget_) {
+        Req* r = queue_.front();
+        queue_.pop_front();
+        resident_ += r->bytes;
+        admit.push_back(r);
+      }
+    }
+    if (!eng) eng = std::make_unique<Engine>(nullptr);
+    for (Req* r : admit) {
+      std::string why;
+      int st = eng->add(&r->world, &r->slot, &why);
+      if (st == OK) st = eng->set_dt(r->slot, r->dt);
+      std::lock_guard<std::mutex> lk(mu_);
+      r->t_admit = Clock::now();
+      if (st != OK) {
+        r->state = SERVE_FAILED;
+        r->error = why.empty() ? eng->last_error : why;
+        resident_ -= r->bytes;
+        ++stats_.failed;
+        finished_.push_back(r->id);
+        continue;
+      }
+      r->state = SERVE_RUNNING;
+      active_.push_back(r);
+      ++stats_.admitted;
+    }
+    std::vector<Req*> act;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      act = active_;
+    }
+    if (act.empty()) continue;
+    // requests that asked for zero steps finish without a tick
+    int st = OK;
+    bool any_steps = false;
+    for (Req* r : act) any_steps |= r->done < r->steps;
+    if (any_steps) {
+      st = eng->step();
+      if (st == OK) st = eng->sync();
+    }
+    uint64_t units = 0;
+    std::vector<Req*> finished;
+    for (Req* r : act) {
+      if (r->done < r->steps) {
+        ++r->done;
+        units += (uint64_t)r->world.particles.size() * r->world.sub_steps;
+      }
+      if (r->done >= r->steps || st != OK) finished.push_back(r);
+    }
+    for (Req* r : finished) {
+      int ds = st == OK ? eng->download(r->slot) : st;
+      eng->remove(r->slot);
+      std::lock_guard<std::mutex> lk(mu_);
+      r->t_done = Clock::now();
+      resident_ -= r->bytes;
+      if (ds != OK) {
+        r->state = SERVE_FAILED;
+        r->error = eng->last_error;
+        ++stats_.failed;
+      } else {
+        r->state = SERVE_DONE;
+        ++stats_.completed;
+      }
+      active_.erase(std::find(active_.begin(), active_.end(), r));
+      finished_.push_back(r->id);
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    ++stats_.ticks;
+    stats_.particle_substeps += units;
+  }
+  eng.reset();
+}
+
+}  // namespace b2d

@@ -1,0 +1,58 @@
+// server.hpp — continuous-batching request loop (see server.cpp).
+#pragma once
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "host.hpp"
+
+namespace b2d {
+
+enum : int { SERVE_QUEUED = 0, SERVE_RUNNING = 1, SERVE_DONE = 2, SERVE_FAILED = 3 };
+
+struct ServerStats {
+  uint64_t submitted = 0, admitted = 0, completed = 0, failed = 0;
+  uint64_t queued = 0, active = 0;
+  uint64_t ticks = 0, particle_substeps = 0;
+  uint64_t resident_bytes = 0;
+};
+
+class Server {
+ public:
+  explicit Server(uint64_t budget_bytes);
+  ~Server();
+  int start();
+  int stop();
+  int submit(const WorldHost& w, uint32_t steps, float dt, uint64_t* id, std::string* why);
+  int poll(uint64_t id, int* state);
+  // hands over a finished request's world and releases the request
+  int take(uint64_t id, WorldHost* out, double* latency_s, double* queue_s, std::string* why);
+  ServerStats stats();
+  static size_t estimate_bytes(const WorldHost& w);
+  // ids of requests finished (done or failed) since the last call
+  std::vector<uint64_t> finished();
+
+ private:
+  struct Req;
+  void loop();
+  uint64_t budget_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  bool running_ = false;
+  std::thread worker_;
+  uint64_t next_id_ = 1;
+  std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs_;
+  std::deque<Req*> queue_;
+  std::vector<Req*> active_;
+  uint64_t resident_ = 0;
+  ServerStats stats_;
+  std::vector<uint64_t> finished_;
+};
+
+}  // namespace b2d

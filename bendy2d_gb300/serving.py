@@ -1,0 +1,148 @@
+"""Serving: continuous batching of world-solve requests (Python side).
+
+``Server`` wraps the native request loop (include/bendy2d.h, b2d_server_*):
+requests are admitted under a device-memory budget, kept device-resident
+across steps, and stepped together.  ``run_poisson`` drives it with seeded
+Poisson arrivals of configuration-4 requests (a config-2-style world of
+log-uniform [64, 16384] particles and a step count uniform in [60, 600]) and
+reports latency percentiles beside throughput.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+import time
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+from .api import Solver
+
+QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+
+class Server:
+    def __init__(self, budget_bytes: int):
+        self._lib = N.load()
+        h = C.c_void_p()
+        N.check(self._lib.b2d_server_create(int(budget_bytes), C.byref(h)))
+        self._h = h
+
+    def start(self) -> None:
+        N.check(self._lib.b2d_server_start(self._h))
+
+    def stop(self) -> None:
+        N.check(self._lib.b2d_server_stop(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.b2d_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, world: Solver, steps: int, dt: float) -> int:
+        rid = C.c_uint64()
+        N.check(self._lib.b2d_server_submit(self._h, world._h, steps, dt, C.byref(rid)))
+        return rid.value
+
+    def poll(self, rid: int) -> int:
+        st = C.c_int()
+        N.check(self._lib.b2d_server_poll(self._h, rid, C.byref(st)))
+        return st.value
+
+    def finished(self, cap: int = 4096) -> list:
+        buf = (C.c_uint64 * cap)()
+        n = C.c_size_t()
+        N.check(self._lib.b2d_server_finished(self._h, buf, cap, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def take(self, rid: int) -> tuple:
+        """(solver holding the final world, latency s, queueing s)"""
+        out = Solver()
+        lat, q = C.c_double(), C.c_double()
+        N.check(self._lib.b2d_server_take(self._h, rid, out._h, C.byref(lat), C.byref(q)))
+        return out, lat.value, q.value
+
+    def stats(self) -> dict:
+        s = N.CServerStats()
+        N.check(self._lib.b2d_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.CServerStats._fields_}
+
+
+def request_pool(n: int, seed: int, lo: int = 64, hi: int = 16384) -> list:
+    """n request worlds with particle counts log-uniform in [lo, hi]."""
+    from . import scenes
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n)).astype(int)
+    return [scenes.config4_request(rng, int(k)) for k in sizes]
+
+
+def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
+                budget_bytes: int = 40 << 30, pool: int = 64, steps_lo: int = 60,
+                steps_hi: int = 600, drain_s: float = 30.0,
+                scenes_pool: Optional[list] = None) -> dict:
+    """Seeded Poisson arrivals for `duration` seconds; waits up to `drain_s`
+    afterwards for outstanding requests.  Latency = submit to completion."""
+    rng = np.random.default_rng(seed + 1)
+    worlds = scenes_pool or request_pool(pool, seed)
+    solvers = [w.to_solver() for w in worlds]
+    gaps = rng.exponential(1.0 / lam, size=int(lam * duration * 1.5) + 16)
+    times = np.cumsum(gaps)
+    times = times[times < duration]
+    picks = rng.integers(0, len(worlds), size=len(times))
+    steps = rng.integers(steps_lo, steps_hi + 1, size=len(times))
+    sv = Server(budget_bytes)
+    sv.start()
+    info = {}
+    lock = threading.Lock()
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k, (t, w, st) in enumerate(zip(times, picks, steps)):
+            delay = t0 + t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            rid = sv.submit(solvers[w], int(st), worlds[w].dt)
+            with lock:
+                info[rid] = (k, int(worlds[w].n_particles) * worlds[w].sub_steps * int(st))
+
+    th = threading.Thread(target=submitter, daemon=True)
+    th.start()
+    lat, qt, done_units = [], [], 0
+    deadline = t0 + duration + drain_s
+    done = 0
+    while True:
+        for rid in sv.finished():
+            s, l, q = sv.take(rid)
+            lat.append(l)
+            qt.append(q)
+            with lock:
+                done_units += info[rid][1]
+            done += 1
+            s.close()
+        if not th.is_alive() and done >= len(times):
+            break
+        if time.perf_counter() > deadline:
+            break
+        time.sleep(0.002)
+    wall = time.perf_counter() - t0
+    stats = sv.stats()
+    sv.stop()
+    sv.close()
+    lat_ms = np.asarray(lat) * 1e3
+    return {
+        "arrival_rate_per_s": lam, "arrival_window_s": duration, "submitted": int(len(times)),
+        "completed": done, "wall_s": wall,
+        "p50_latency_ms": float(np.percentile(lat_ms, 50)) if done else None,
+        "p99_latency_ms": float(np.percentile(lat_ms, 99)) if done else None,
+        "mean_queue_ms": float(np.mean(qt) * 1e3) if done else None,
+        "throughput_particle_substeps_per_s": stats["particle_substeps"] / wall,
+        "completed_particle_substeps_per_s": done_units / wall,
+        "ticks": stats["ticks"], "budget_bytes": budget_bytes,
+    }

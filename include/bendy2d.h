@@ -199,6 +199,37 @@ int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out);
  * graph) — the one-world-per-launch baseline the batched path is compared to */
 int b2d_batch_set_plain(b2d_batch* b, int on);
 
+/* ---- serving: continuous batching of world-solve requests -------------- */
+/* A request is a copy of a solver's world plus a number of Solver::update
+ * calls (src/solver.rs:106-116).  A worker thread admits queued requests
+ * first come first served while the device bytes of resident worlds stay
+ * within the budget, steps every resident world once per tick in one launch
+ * sequence, and retires finished requests.  Results are bit-identical to
+ * running the request alone. */
+#define B2D_SERVE_QUEUED 0
+#define B2D_SERVE_RUNNING 1
+#define B2D_SERVE_DONE 2
+#define B2D_SERVE_FAILED 3
+typedef struct {
+  uint64_t submitted, admitted, completed, failed, queued, active;
+  uint64_t ticks, particle_substeps, resident_bytes;
+} b2d_server_stats;
+int b2d_server_create(uint64_t budget_bytes, b2d_server** out);
+int b2d_server_destroy(b2d_server* sv);
+int b2d_server_start(b2d_server* sv);
+int b2d_server_stop(b2d_server* sv);
+/* B2D_ERR_BUDGET when the world alone exceeds the budget */
+int b2d_server_submit(b2d_server* sv, b2d_solver* world, uint32_t steps, float dt,
+                      uint64_t* id);
+int b2d_server_poll(b2d_server* sv, uint64_t id, int* state);
+/* moves a finished request's world into dst (replacing its contents) and
+ * releases the request; latency from submit to completion, queueing time */
+int b2d_server_take(b2d_server* sv, uint64_t id, b2d_solver* dst, double* latency_s,
+                    double* queue_s);
+/* ids of requests finished (done or failed) since the last call, at most cap */
+int b2d_server_finished(b2d_server* sv, uint64_t* ids, size_t cap, size_t* n);
+int b2d_server_get_stats(b2d_server* sv, b2d_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif
