@@ -218,6 +218,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--serve-window", type=float, default=1.0)
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -364,6 +366,15 @@ def main():
     batched = None
     if not args.no_batched and world == 1:
         batched = run_batched_comparison(args, torch, flush, stream)
+    serving = None
+    if not args.no_serve and world == 1:
+        from bendy2d_gb300.serving import run_poisson
+        serving = run_poisson(lam=2000.0, duration=args.serve_window, seed=0,
+                              budget_bytes=40 << 30, pool=64, drain_s=120.0)
+        serving["workload"] = ("Poisson arrivals at 2000 req/s for the window, worlds of "
+                               "log-uniform [64, 16384] particles built like configuration 2 "
+                               "(grids, particle collisions), steps uniform in [60, 600], "
+                               "dt 1/60, 8 sub-steps, 40 GB budget")
 
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -386,6 +397,7 @@ def main():
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "batched_config3": batched,
+        "serving_config4": serving,
     }
     print(json.dumps(out))
     if world > 1:
