@@ -199,6 +199,50 @@ def run_batched_comparison(args, torch, flush, stream):
     return out
 
 
+def link_residual(solver, sc) -> dict:
+    """|len - rest| / rest over the particle links (float64 on the host):
+    max, 99th percentile and median"""
+    p, _ = solver.read_state()
+    a, b = sc.la.astype(np.int64), sc.lb.astype(np.int64)
+    d = np.linalg.norm(p[a].astype(np.float64) - p[b], axis=1)
+    r = np.abs(d - sc.rest) / sc.rest
+    return {"max": float(r.max()), "p99": float(np.percentile(r, 99)),
+            "median": float(np.median(r))}
+
+
+def run_config5(args, torch, flush, stream):
+    """Configuration 5: 1024 cloth grids (1,048,576 particles, 3,999,744 links),
+    20 sub-steps, 8 link iterations, particle collisions, 64 circles, 32
+    polygons; fast coloured mode against reference order, with residuals."""
+    from bendy2d_gb300 import MODE_FAST, MODE_REFERENCE, scenes
+    out = {"workload": "1024 cloth grids 32x32 (1,048,576 particles, 3,999,744 links) in "
+                       "4000^2, 20 sub-steps, 8 link iterations, particle collisions, 64 static "
+                       "circles, 32 static polygons", "steps": args.config5_steps}
+    for name, mode in (("fast", MODE_FAST), ("reference_order", MODE_REFERENCE)):
+        sc = scenes.config5(seed=0, mode=mode)
+        s = sc.to_solver()
+        s.set_stream(stream.cuda_stream)
+        s.update(sc.dt)
+        s.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.config5_steps)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                s.update(sc.dt)
+                e1.record(stream)
+        s.synchronize()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+        out[name] = {"value": sc.n_particles * sc.sub_steps / (ms / 1e3), "ms_per_step": ms,
+                     "residual_after": link_residual(s, sc),
+                     "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024}
+        s.close()
+    return out
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -219,6 +263,8 @@ def main():
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--serve-window", type=float, default=1.0)
+    ap.add_argument("--config5-steps", type=int, default=5)
+    ap.add_argument("--no-config5", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_env()
@@ -366,6 +412,9 @@ def main():
     batched = None
     if not args.no_batched and world == 1:
         batched = run_batched_comparison(args, torch, flush, stream)
+    config5 = None
+    if not args.no_config5 and world == 1:
+        config5 = run_config5(args, torch, flush, stream)
     serving = None
     if not args.no_serve and world == 1:
         from bendy2d_gb300.serving import run_poisson
@@ -398,6 +447,7 @@ def main():
         "cpu_baseline": cpu,
         "batched_config3": batched,
         "serving_config4": serving,
+        "stress_config5": config5,
     }
     print(json.dumps(out))
     if world > 1:

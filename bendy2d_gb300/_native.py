@@ -137,6 +137,7 @@ SIGNATURES = {
     "b2d_batch_get_profile": [_P, C.c_char_p, C.c_size_t, _F, C.c_size_t, _SZ],
     "b2d_batch_get_launch_count": [_P, C.POINTER(C.c_uint32)],
     "b2d_batch_set_plain": [_P, C.c_int],
+    "b2d_batch_set_tuning": [_P, C.c_char_p, C.c_double],
     "b2d_server_create": [C.c_uint64, C.POINTER(_P)],
     "b2d_server_destroy": [_P],
     "b2d_server_start": [_P],

@@ -452,6 +452,10 @@ class Batch:
         N.check(self._lib.b2d_batch_get_launch_count(self._h, C.byref(v)))
         return v.value
 
+    def set_tuning(self, **kv) -> None:
+        for k, v in kv.items():
+            N.check(self._lib.b2d_batch_set_tuning(self._h, k.encode(), float(v)))
+
     def set_plain(self, on: bool) -> None:
         """One-world-per-launch baseline: no batching, no CUDA graph."""
         N.check(self._lib.b2d_batch_set_plain(self._h, int(on)))

@@ -90,6 +90,7 @@ struct DWorld {
   float4* paabb;
   uint2* plab; float* plrest;
   uint32_t* stage_off;   // polygon-pair test offsets, see rigid_phase_a
+  uint32_t* stage_pr;    // polygon pair of each stage: self | other << 16
 };
 
 // Shared (engine-wide) read-only schedule registry, plus the device error

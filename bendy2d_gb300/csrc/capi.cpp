@@ -56,6 +56,8 @@ struct b2d_batch {
   cudaStream_t stream = nullptr;
   bool profiling = false;
   bool plain = false;
+  PlanTuning tune;
+  bool tune_set = false;
 };
 
 static int have_gpu() {
@@ -70,6 +72,7 @@ static int engine_for(b2d_solver* s, Engine** out) {
       if (!have_gpu()) return fail(ERR_CUDA, "no CUDA device: bendy2d-gb300 has no CPU path");
       s->batch->eng = std::make_unique<Engine>(s->batch->stream);
       s->batch->eng->set_plain(s->batch->plain);
+      if (s->batch->tune_set) s->batch->eng->set_tuning(s->batch->tune);
     }
     *out = s->batch->eng.get();
     return OK;
@@ -693,6 +696,19 @@ int b2d_batch_get_profile(b2d_batch* b, char* names, size_t names_cap, float* ms
                           size_t* count) {
   if (!b) return fail(ERR_NULL, "null batch");
   return put_profile(b->eng.get(), names, names_cap, ms, cap, count);
+}
+int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value) {
+  if (!b || !key) return fail(ERR_NULL, "null argument");
+  if (!b->tune.set(key, value)) return fail(ERR_ARG, std::string("unknown tunable: ") + key);
+  b->tune_set = true;
+  if (b->eng) {
+    for (b2d_solver* s : b->members) {
+      int st = unplace(s);
+      if (st != OK) return st;
+    }
+    b->eng->set_tuning(b->tune);
+  }
+  return OK;
 }
 int b2d_batch_set_plain(b2d_batch* b, int on) {
   if (!b) return fail(ERR_NULL, "null batch");

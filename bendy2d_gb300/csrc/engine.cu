@@ -167,6 +167,7 @@ int Engine::fill_world_record(uint32_t slot) {
   W.plab = reinterpret_cast<uint2*>(b + L.o_plab);
   W.plrest = reinterpret_cast<float*>(b + L.o_plrest);
   W.stage_off = reinterpret_cast<uint32_t*>(b + L.o_stage);
+  W.stage_pr = reinterpret_cast<uint32_t*>(b + L.o_stage_pr);
   W.h = s.dt * (1.0f / (float)W.S);  // src/solver.rs:107-108
   if (h_worlds_.size() <= slot) h_worlds_.resize(slot + 1);
   h_worlds_[slot] = W;
@@ -465,7 +466,7 @@ int Engine::rebuild_lists() {
       const uint64_t ng = im.polys.size(), nc = im.cpos.size(), nv = im.vpos.size();
       // same expression as rigid_smem_bytes() in kernels.cuh
       const uint64_t need = 48 * ng + 28 * nc + 12 * im.clab.size() + 24 * nv +
-                            12 * im.plab.size() + 4 * im.stage_off.size() + 256;
+                            12 * im.plab.size() + 8 * im.stage_off.size() + 272;
       if (need <= kRigidSmemCap) rigid_smem = std::max<uint64_t>(rigid_smem, need);
     }
     if (full) {
@@ -650,7 +651,7 @@ int Engine::launch_all(bool profiling) {
       }
       if (wl.rigid >= 0) {
         timed("plain_rigid", [&] {
-          k_rigid<0><<<1, 128, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
+          k_rigid<0><<<1, 256, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
         });
       }
     }
@@ -673,7 +674,7 @@ int Engine::launch_all(bool profiling) {
   }
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
-    timed("rigid_full", [&] { k_rigid<0><<<n, 128, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
+    timed("rigid_full", [&] { k_rigid<0><<<n, 256, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
   }
   }
   // worlds with extension collisions: per sub-step pipeline
@@ -685,8 +686,8 @@ int Engine::launch_all(bool profiling) {
     const uint32_t cur = s & 1u;
     if (nre) {  // phase B of s-1 (after collide s-1 read the circles), phase A of s
       timed("rigid_ext", [&] {
-        if (s == 0) k_rigid<1><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
-        else k_rigid<3><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        if (s == 0) k_rigid<1><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        else k_rigid<3><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
       });
     }
     groups(false, cur, s);
@@ -728,7 +729,7 @@ int Engine::launch_all(bool profiling) {
     if (nre) edge(stream_, ax);
   }
   if (smax_ext_ > 0) {
-    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 128, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
+    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
     timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
   }
   edge(ax, stream_);

@@ -71,6 +71,7 @@ struct WorldImage {
   std::vector<uint2> plab;
   std::vector<float> plrest;
   std::vector<uint32_t> stage_off;
+  std::vector<uint32_t> stage_pr;
   std::vector<GroupBody> groups;
   std::vector<uint32_t> serials;
   std::vector<uint32_t> link_order;  // fast mode: world link order used
@@ -86,7 +87,7 @@ struct BlockLayout {
   size_t state_bytes = 0, total = 0;
   size_t o_pos, o_prev, o_cpos, o_cprev, o_cacc, o_vpos, o_vprev, o_vacc, o_pcenter;
   size_t o_pos1, o_bidx, o_bodies, o_lab, o_lrest, o_lstiff, o_crad, o_cstatic, o_clab,
-      o_clrest, o_polys, o_paabb, o_plab, o_plrest, o_stage;
+      o_clrest, o_polys, o_paabb, o_plab, o_plrest, o_stage, o_stage_pr;
 };
 BlockLayout layout_of(const WorldImage& im);
 void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst);

@@ -582,29 +582,28 @@ __device__ __forceinline__ uint64_t pair_row_off(uint64_t i, uint64_t n) {
   return i * (2 * n - i - 1) / 2;
 }
 // k-th pair (i<j) in row-major order over n items
+// k-th pair (i<j) in row-major order over n items: binary search for the
+// last row whose first pair index is <= k (integer arithmetic only)
 __device__ __forceinline__ void unrank_pair(uint64_t k, uint32_t n, uint32_t& i, uint32_t& j) {
-  double dn = (double)n;
-  double disc = (2.0 * dn - 1.0) * (2.0 * dn - 1.0) - 8.0 * (double)k;
-  if (disc < 0.0) disc = 0.0;
-  int64_t x = (int64_t)((2.0 * dn - 1.0 - sqrt(disc)) * 0.5);
-  if (x < 0) x = 0;
-  if (x > (int64_t)n - 2) x = (int64_t)n - 2;
-  uint64_t ii = (uint64_t)x;
-  while (ii > 0 && pair_row_off(ii, n) > k) --ii;
-  while (ii + 1 < n && pair_row_off(ii + 1, n) <= k) ++ii;
-  i = (uint32_t)ii;
-  j = (uint32_t)(k - pair_row_off(ii, n) + ii + 1);
+  uint32_t lo = 0, hi = n - 1;  // row in [lo, hi)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (pair_row_off(mid, n) <= k) lo = mid; else hi = mid;
+  }
+  i = lo;
+  j = (uint32_t)(k - pair_row_off(lo, n) + lo + 1);
 }
 
 // Polygon pair "stages": stage s = (self, other) in reference order (pairs
 // i<j row-major; (i,j) then (j,i)).  Test x within a stage is (edge e of
 // self, point q of other), numbered e*nv_other + q.  The host stores
-// stage_off[s] = first test of stage s, and the total after the last stage.
-__device__ __forceinline__ void stage_pair(uint32_t s, uint32_t ng, uint32_t& self,
+// stage_off[s] = first test of stage s (and the total after the last stage)
+// and stage_pr[s] = self | other << 16.
+__device__ __forceinline__ void stage_pair(const uint32_t* pr, uint32_t s, uint32_t& self,
                                            uint32_t& other) {
-  uint32_t i, j;
-  unrank_pair(s >> 1, ng, i, j);
-  if (s & 1) { self = j; other = i; } else { self = i; other = j; }
+  const uint32_t v = pr[s];  // self | other << 16, precomputed on the host
+  self = v & 0xFFFFu;
+  other = v >> 16;
 }
 
 __device__ __forceinline__ uint32_t stage_of(const uint32_t* so, uint32_t nstage, uint32_t x) {
@@ -621,7 +620,7 @@ struct RigidView {
   float2* cp; float2* cq; float2* ca; float* cr; uint32_t* cst;
   uint2* clab; float* clrest;
   DPoly* polys; float2* vpos; float2* vprev; float2* vacc; float2* pcenter; float4* paabb;
-  uint2* plab; float* plrest; uint32_t* stage_off;
+  uint2* plab; float* plrest; uint32_t* stage_off; uint32_t* stage_pr;
   uint32_t nc, ncl, ng, nv, npl, nst;
 };
 
@@ -632,6 +631,7 @@ __device__ __forceinline__ RigidView global_view(const DWorld& W) {
   v.polys = W.polys; v.vpos = W.vpos; v.vprev = W.vprev; v.vacc = W.vacc;
   v.pcenter = W.pcenter; v.paabb = W.paabb; v.plab = W.plab; v.plrest = W.plrest;
   v.stage_off = W.stage_off;
+  v.stage_pr = W.stage_pr;
   v.nc = W.nc; v.ncl = W.ncl; v.ng = W.ng;
   v.nv = W.ng ? W.polys[W.ng - 1].v0 + W.polys[W.ng - 1].nv : 0u;
   v.npl = W.ng ? W.polys[W.ng - 1].l0 + W.polys[W.ng - 1].nl : 0u;
@@ -641,7 +641,7 @@ __device__ __forceinline__ RigidView global_view(const DWorld& W) {
 
 __device__ __forceinline__ uint32_t rigid_smem_bytes(const RigidView& v) {
   // payload plus 16-byte rounding of the 16 pieces (stage_view)
-  return 48u * v.ng + 28u * v.nc + 12u * v.ncl + 24u * v.nv + 12u * v.npl + 4u * v.nst + 256u;
+  return 48u * v.ng + 28u * v.nc + 12u * v.ncl + 24u * v.nv + 12u * v.npl + 8u * v.nst + 272u;
 }
 
 // carve a shared-memory view (16-byte aligned pieces first)
@@ -665,6 +665,7 @@ __device__ __forceinline__ RigidView stage_view(const RigidView& g, unsigned cha
   v.clrest = reinterpret_cast<float*>(take(4u * g.ncl));
   v.plrest = reinterpret_cast<float*>(take(4u * g.npl));
   v.stage_off = reinterpret_cast<uint32_t*>(take(4u * g.nst));
+  v.stage_pr = reinterpret_cast<uint32_t*>(take(4u * g.nst));
   return v;
 }
 
@@ -686,6 +687,7 @@ __device__ __forceinline__ void copy_view(const RigidView& d, const RigidView& s
     for (uint32_t i = tid; i < s.ncl; i += nt) { d.clab[i] = s.clab[i]; d.clrest[i] = s.clrest[i]; }
     for (uint32_t i = tid; i < s.npl; i += nt) { d.plab[i] = s.plab[i]; d.plrest[i] = s.plrest[i]; }
     for (uint32_t i = tid; i < s.nst; i += nt) d.stage_off[i] = s.stage_off[i];
+    for (uint32_t i = tid + 1; i < s.nst; i += nt) d.stage_pr[i - 1] = s.stage_pr[i - 1];
   }
 }
 
@@ -781,7 +783,7 @@ __device__ __forceinline__ void rigid_phase_a(const DWorld& W, const RigidView& 
       if (x < total) {
         const uint32_t st = stage_of(so, nstage, x);
         uint32_t self, other;
-        stage_pair(st, W.ng, self, other);
+        stage_pair(R.stage_pr, st, self, other);
         const DPoly PS = polys[self], PO = polys[other];
         const uint32_t r = x - so[st];
         const uint32_t e = r / PO.nv;
@@ -805,7 +807,7 @@ __device__ __forceinline__ void rigid_phase_a(const DWorld& W, const RigidView& 
       if (tid == 0) {
         const uint32_t st = stage_of(so, nstage, f);
         uint32_t self, other;
-        stage_pair(st, W.ng, self, other);
+        stage_pair(R.stage_pr, st, self, other);
         const DPoly PS = polys[self], PO = polys[other];
         const uint32_t e = (f - so[st]) / PO.nv;
         const uint32_t b = (e + 1) % PS.nv;
@@ -907,7 +909,7 @@ __device__ __forceinline__ void rigid_phase_b(const DWorld& W, const RigidView& 
 // in `smem_bytes` (serial chains then cost shared-memory latency), else the
 // phases run on global memory.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_rigid(const DWorld* __restrict__ worlds,
+__global__ void __launch_bounds__(256) k_rigid(const DWorld* __restrict__ worlds,
                                                const uint32_t* __restrict__ wlist, uint32_t n,
                                                uint32_t sub, uint32_t smem_bytes) {
   extern __shared__ __align__(16) unsigned char rsm[];
@@ -1173,19 +1175,58 @@ __device__ __forceinline__ void visit_cell(const DGrid& G, const DWorld& W, uint
 // Particle collisions + bounds + integrate of one sub-step of the extension
 // pipeline.  Reads positions from buffer cur (the post-link snapshot) and
 // writes the new ones to buffer cur^1; prev is updated in place.
-static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWorld* __restrict__ worlds,
-                                                             DGrid G, const uint2* __restrict__ chunks,
-                                                             uint32_t nchunks, uint32_t cur,
-                                                             uint32_t sub) {
+// True when the interval [lo, hi] cannot reach [cmin, cmax] even allowing
+// for float rounding in the exact per-particle test (a relative margin of
+// 1e-5 is far above the few-ulp error of the subtractions and squares there).
+__device__ __forceinline__ bool separated(float lo, float hi, float cmin, float cmax) {
+  const float d = 1e-5f * (fabsf(lo) + fabsf(hi) + 1.0f);
+  return cmax < lo - d || cmin > hi + d;
+}
+
+// min/max of the CTA's particle positions (NaN ignored)
+__device__ __forceinline__ float4 block_box(bool act, float2 p) {
+  __shared__ float4 wbox[CHUNK / 32];
+  float4 b = act ? make_float4(p.x, p.y, p.x, p.y)
+                 : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    b.x = fminf(b.x, __shfl_xor_sync(0xFFFFFFFFu, b.x, o));
+    b.y = fminf(b.y, __shfl_xor_sync(0xFFFFFFFFu, b.y, o));
+    b.z = fmaxf(b.z, __shfl_xor_sync(0xFFFFFFFFu, b.z, o));
+    b.w = fmaxf(b.w, __shfl_xor_sync(0xFFFFFFFFu, b.w, o));
+  }
+  if ((threadIdx.x & 31u) == 0) wbox[threadIdx.x >> 5] = b;
+  __syncthreads();
+  b = wbox[0];
+  for (uint32_t w = 1; w < blockDim.x / 32; ++w) {
+    const float4 c = wbox[w];
+    b.x = fminf(b.x, c.x); b.y = fminf(b.y, c.y);
+    b.z = fmaxf(b.z, c.z); b.w = fmaxf(b.w, c.w);
+  }
+  __syncthreads();
+  return b;
+}
+
+// Particle collisions + bounds + integrate of one sub-step of the extension
+// pipeline.  Reads positions from buffer cur (the post-link snapshot) and
+// writes the new ones to buffer cur^1; prev is updated in place.  A CTA is
+// one chunk of one world.  Circle and polygon tests are skipped for the whole
+// CTA when no circle or polygon box reaches the CTA's particles: then no
+// particle is in contact, nothing moves, and so no later test of the
+// sequence can hit either — the skip is exact.
+static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(
+    const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
+    uint32_t nchunks, uint32_t cur, uint32_t sub) {
   if (blockIdx.x >= nchunks) return;
   const uint2 ch = chunks[blockIdx.x];
   const DWorld& W = worlds[ch.x];
+  if (sub >= W.S) return;  // uniform over the CTA
   const uint32_t i = ch.y + threadIdx.x;
-  if (i >= W.np || sub >= W.S) return;
+  const bool act = i < W.np;
   const float2* P = W.pos[cur];
-  float2 p = P[i];
-  float2 q = W.prev[i];
-  if (W.flags & COLLIDE_PP) {
+  float2 p = act ? P[i] : make_float2(0.f, 0.f);
+  float2 q = act ? W.prev[i] : make_float2(0.f, 0.f);
+  if ((W.flags & COLLIDE_PP) && act) {
     const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
     const float D = fadd(W.radius, W.radius);
     const float D2 = fmul(D, D);
@@ -1211,10 +1252,34 @@ static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(const DWo
     visit_cell(G, W, i, p, cx + 1, cy + 1, r8.x, r8.y, D, D2, sx, sy, hit);
     if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
   }
-  if (W.flags & COLLIDE_PC) p = particle_circles(W, p);
-  if (W.flags & COLLIDE_PPOLY) {
-    for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
+  const uint32_t flags = W.flags;
+  if (flags & (COLLIDE_PC | COLLIDE_PPOLY)) {
+    const float4 box = block_box(act, p);
+    bool near = false;
+    if (flags & COLLIDE_PC) {
+      for (uint32_t k = threadIdx.x; k < W.nc; k += blockDim.x) {
+        const float2 c = W.cpos[k];
+        const float R = W.radius + W.crad[k];
+        near |= !(separated(c.x - R, c.x + R, box.x, box.z) ||
+                  separated(c.y - R, c.y + R, box.y, box.w));
+      }
+    }
+    if (flags & COLLIDE_PPOLY) {
+      for (uint32_t k = threadIdx.x; k < W.ng; k += blockDim.x) {
+        const float4 bb = W.paabb[k];
+        const float r = W.radius;
+        near |= !(separated(bb.x - r, bb.z + r, box.x, box.z) ||
+                  separated(bb.y - r, bb.w + r, box.y, box.w));
+      }
+    }
+    if (__syncthreads_or(near) && act) {
+      if (flags & COLLIDE_PC) p = particle_circles(W, p);
+      if (flags & COLLIDE_PPOLY) {
+        for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
+      }
+    }
   }
+  if (!act) return;
   solve_bounds(p, q, W);
   integrate(p, q, W.gx, W.gy, W.h);
   W.pos[cur ^ 1u][i] = p;

@@ -202,6 +202,9 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
   }
   const size_t nst = P.ng >= 2 ? (size_t)P.ng * (P.ng - 1) + 1 : 0;
   if (im.stage_off.size() != nst) return bad("polygon stage table");
+  if (im.stage_pr.size() != (nst ? nst - 1 : 0)) return bad("polygon stage pairs");
+  for (uint32_t v : im.stage_pr)
+    if ((v & 0xFFFFu) >= P.ng || (v >> 16) >= P.ng) return bad("polygon stage pair");
   for (size_t i = 1; i < nst; ++i)
     if (im.stage_off[i] < im.stage_off[i - 1]) return bad("polygon stage order");
   return true;
@@ -444,11 +447,17 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
   // polygon pair stages: (i,j) then (j,i) for pairs i<j in row-major order
   if (P.ng >= 2) {
     uint32_t acc = 0;
+    if (P.ng > 65535u) {
+      if (why) *why = "at most 65535 polygons per world";
+      return ERR_ARG;
+    }
     for (uint32_t i = 0; i < P.ng; ++i)
       for (uint32_t j = i + 1; j < P.ng; ++j) {
         im.stage_off.push_back(acc);
+        im.stage_pr.push_back(i | (j << 16));
         acc += im.polys[i].nv * im.polys[j].nv;
         im.stage_off.push_back(acc);
+        im.stage_pr.push_back(j | (i << 16));
         acc += im.polys[j].nv * im.polys[i].nv;
       }
     im.stage_off.push_back(acc);
@@ -494,6 +503,7 @@ BlockLayout layout_of(const WorldImage& im) {
   L.o_plab = seg(8 * im.plab.size());
   L.o_plrest = seg(4 * im.plrest.size());
   L.o_stage = seg(4 * im.stage_off.size());
+  L.o_stage_pr = seg(4 * im.stage_pr.size());
   L.total = std::max<size_t>(o, 16);
   return L;
 }
@@ -526,6 +536,7 @@ void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst)
   put(L.o_plab, im.plab.data(), 8 * im.plab.size());
   put(L.o_plrest, im.plrest.data(), 4 * im.plrest.size());
   put(L.o_stage, im.stage_off.data(), 4 * im.stage_off.size());
+  put(L.o_stage_pr, im.stage_pr.data(), 4 * im.stage_pr.size());
 }
 
 }  // namespace b2d

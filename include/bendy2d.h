@@ -198,6 +198,8 @@ int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out);
 /* plain mode: each member world gets its own launches (no batching, no CUDA
  * graph) — the one-world-per-launch baseline the batched path is compared to */
 int b2d_batch_set_plain(b2d_batch* b, int on);
+/* executor tunables for every member (see b2d_set_tuning); re-plans members */
+int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
 
 /* ---- serving: continuous batching of world-solve requests -------------- */
 /* A request is a copy of a solver's world plus a number of Solver::update
