@@ -17,8 +17,25 @@ namespace b2d {
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// IEEE division and square root with exact zero shortcuts.  Measured on
+// sm_103a, __fdiv_rn with a zero numerator takes ~250 cycles against ~55 for
+// ordinary operands, and __fsqrt_rn(0) ~130 against ~53; axis-aligned links
+// (dx or dy exactly 0) hit that case on most ops.  IEEE 754 fixes those
+// results exactly: ±0 / d = ±0 for d > 0 and ∓0 for d < 0 (d not NaN, any
+// magnitude including infinity), and sqrt(±0) = ±0.  They are selected
+// without executing the operation on a zero (the operation sees 1 instead),
+// so every result is bit-identical to the plain intrinsic.
+__device__ __forceinline__ float fdiv(float a, float b) {
+  const bool z = (a == 0.0f) && (b > 0.0f || b < 0.0f);
+  const float q = __fdiv_rn(z ? 1.0f : a, b);
+  return z ? (b > 0.0f ? a : -a) : q;
+}
+__device__ __forceinline__ float fsqrt(float a) {
+  const bool z = a == 0.0f;
+  const float r = __fsqrt_rn(z ? 1.0f : a);
+  return z ? a : r;
+}
 
 // nalgebra norm_squared is 0 + (x*x + y*y); a sum of two squares is never
 // -0, so adding the leading +0 cannot change the value and is omitted.
@@ -212,13 +229,18 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   const uint32_t sq_a = sp_a + 8u * B.np;
   const uint32_t srs_a = sq_a + (FULL ? 8u * B.np : 0u);
   if (SMEM) {
+    // plain stores here, so the compiler can keep many global loads in flight
+    float2* sp = reinterpret_cast<float2*>(base);
+    float2* sq = sp + B.np;
+    float2* srs = sq + (FULL ? B.np : 0u);
+#pragma unroll 4
     for (uint32_t i = t; i < B.np; i += T) {
       const uint32_t k = bidx[i];
-      sts_f32x2(sp_a + 8u * i, gp[k]);
-      if (FULL) sts_f32x2(sq_a + 8u * i, gq[k]);
+      sp[i] = gp[k];
+      if (FULL) sq[i] = gq[k];
     }
-    for (uint32_t i = t; i < B.nl; i += T)
-      sts_f32x2(srs_a + 8u * i, make_float2(grest[i], gstiff[i]));
+#pragma unroll 4
+    for (uint32_t i = t; i < B.nl; i += T) srs[i] = make_float2(grest[i], gstiff[i]);
   }
   group_sync(g, T);
 
@@ -246,18 +268,9 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     const uint32_t buf_a = cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u;
     const uint32_t nseg = lds_u32(buf_a);
     const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
-    // The op stream is immutable: each thread fetches the next segment's end,
-    // its first op there and that link's {rest, stiffness} before the
-    // barrier, so after it only the position loads remain on the path.
-    auto fetch_op = [&](uint32_t k, uint32_t e) {
-      return k < e ? lds_u32x2(ops_a + 8u * k) : make_uint2(0u, OP_NONE);
-    };
-    auto fetch_rs = [&](uint2 op) {
-      return (SMEM && op.y < OP_INTEG) ? lds_f32x2(srs_a + 8u * op.y) : make_float2(0.f, 0.f);
-    };
-    auto run = [&](uint2 op, float2 rs) {
-      if (op.y == OP_NONE) return;
-      if (op.y == OP_INTEG) {
+    // One op: a link solve or (FULL) bounds + integrate of one particle.
+    auto run = [&](uint2 op) {
+      if (FULL && op.y == OP_INTEG) {
         float2 p, q;
         if (SMEM) {
           p = lds_f32x2(sp_a + 8u * op.x);
@@ -276,6 +289,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
           gq[bidx[op.x]] = q;
         }
       } else if (SMEM) {
+        const float2 rs = lds_f32x2(srs_a + 8u * op.y);
         const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
         float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
         link_solve(pa, pb, rs.x, rs.y);
@@ -298,36 +312,26 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
         gp[ib] = pb;
       }
     };
+    // Segment loop: the segment's ops go to the group's threads in turn,
+    // then the group barrier.  (Prefetching the next segment's op ahead of
+    // the barrier measured slower than this plain form.)
     uint32_t beg = 0;
-    uint32_t end = lds_u32(buf_a + 4u);
-    uint2 op = fetch_op(t, end);
-    float2 rs = fetch_rs(op);
     for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
-      uint32_t end_n = end;
-      uint2 op_n = make_uint2(0u, OP_NONE);
-      if (sgi + 1 < nseg) {
-        end_n = lds_u32(buf_a + 8u + 4u * sgi);
-        op_n = fetch_op(end + t, end_n);
-      }
-      run(op, rs);
-      for (uint32_t k = beg + t + T; k < end; k += T) {
-        const uint2 o2 = lds_u32x2(ops_a + 8u * k);
-        run(o2, fetch_rs(o2));
-      }
-      const float2 rs_n = fetch_rs(op_n);
+      const uint32_t end = lds_u32(buf_a + 4u + 4u * sgi);
+      for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
       group_sync(g, T);
       beg = end;
-      end = end_n;
-      op = op_n;
-      rs = rs_n;
     }
   }
 
   if (SMEM) {
+    const float2* sp = reinterpret_cast<const float2*>(base);
+    const float2* sq = sp + B.np;
+#pragma unroll 4
     for (uint32_t i = t; i < B.np; i += T) {
       const uint32_t k = bidx[i];
-      gp[k] = lds_f32x2(sp_a + 8u * i);
-      if (FULL) gq[k] = lds_f32x2(sq_a + 8u * i);
+      gp[k] = sp[i];
+      if (FULL) gq[k] = sq[i];
     }
   }
 }
