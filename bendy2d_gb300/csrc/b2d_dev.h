@@ -102,18 +102,21 @@ struct DScheds {
   const uint32_t* stream;
   uint32_t* err;
 };
-enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u };
+enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_SCAN_TIMEOUT = 2u };
 
 // Extension broadphase: hashed uniform grid built by a counting sort each
 // sub-step.  Every world with particle collisions owns a power-of-two range
 // of buckets; a bucket's entries are contiguous in `sorted`.
 constexpr uint32_t SCAN_TILE = 4096;  // buckets per scan block (1024 threads x 4)
 struct DGrid {
-  uint32_t* count;       // nbuckets: entries per bucket
+  uint32_t* count;       // nbuckets: entries per bucket (all zero between sub-steps)
   uint2* range;          // nbuckets: {exclusive prefix sum of count, count}
-  uint32_t* partial;     // per scan tile: sum of its counts
+  unsigned long long* tstate;  // per scan tile: {epoch << 2 | kind, value}, kind 1 = tile
+                               // sum, 2 = inclusive prefix (decoupled look-back)
+  uint32_t* tctl;        // scan control: [0] next tile id, [1] tiles done, [2] epoch
   uint2* pbr;            // per particle: (bucket, rank within bucket)
-  uint4* sorted;         // per particle: {pos.x bits, pos.y bits, particle, cell x}
+  uint4* sorted;         // per particle: {pos.x bits, pos.y bits, cell x, cell y}
+  uint32_t* err;         // device error word (ERR_BIT_*)
   uint32_t nbuckets;
 };
 

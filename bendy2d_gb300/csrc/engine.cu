@@ -319,6 +319,7 @@ int Engine::check_device_error() {
   B2D_CUDA(cudaMemcpyAsync(&e, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
   B2D_CUDA(cudaStreamSynchronize(stream_));
   if (e) {
+    grid_reset_ = true;
     B2D_CUDA(cudaMemsetAsync(d_err_, 0, 4, stream_));
     last_error = "device error word " + std::to_string(e) +
                  ((e & ERR_BIT_TMA_TIMEOUT) ? " (a bulk-copy wait timed out)" : "");
@@ -334,8 +335,8 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   const size_t ntiles = (nb + SCAN_TILE - 1) / SCAN_TILE;
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
-  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_part = seg(ntiles * 4),
-               o_pbr = seg(np * 8), o_sorted = seg(np * 16);
+  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_tstate = seg(ntiles * 8),
+               o_tctl = seg(16), o_pbr = seg(np * 8), o_sorted = seg(np * 16);
   B2D_CUDA(cudaStreamSynchronize(stream_));
   if (d_grid_) dev_bytes_ -= grid_bytes_;
   cudaFree(d_grid_);
@@ -344,12 +345,15 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
   grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
   grid_.range = reinterpret_cast<uint2*>(d_grid_ + o_start);
-  grid_.partial = reinterpret_cast<uint32_t*>(d_grid_ + o_part);
+  grid_.tstate = reinterpret_cast<unsigned long long*>(d_grid_ + o_tstate);
+  grid_.tctl = reinterpret_cast<uint32_t*>(d_grid_ + o_tctl);
   grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o_pbr);
   grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o_sorted);
   grid_.nbuckets = (uint32_t)nb;
   grid_np_ = np;
   grid_bytes_ = bytes;
+  grid_head_bytes_ = o_pbr;
+  grid_reset_ = false;
   dev_bytes_ += bytes;
   invalidate_graph();
   return OK;
@@ -586,6 +590,7 @@ int Engine::launch_all(bool profiling) {
     }
   };
   const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_};
+  grid_.err = d_err_;
   const DWorld* W = d_worlds_;
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
@@ -706,25 +711,19 @@ int Engine::launch_all(bool profiling) {
       });
     }
     if (any_pp_) {
+      // counts are all zero here: the scan of the previous sub-step cleared them
       const uint32_t nt = (grid_used_ + SCAN_TILE - 1) / SCAN_TILE;
-      timed("grid_clear", [&] {
-        cudaMemsetAsync(grid_.count, 0, (size_t)grid_used_ * 4, stream_);
-      }, false);
       timed("grid_count", [&] {
         k_grid_count<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });
-      timed("grid_scan", [&] {
-        k_scan_reduce<<<nt, 1024, 0, stream_>>>(grid_, grid_used_);
-        k_scan_apply<<<nt, 1024, 0, stream_>>>(grid_, grid_used_);
-      });
-      ++launches_;
+      timed("grid_scan", [&] { k_grid_scan<<<nt, 1024, 0, stream_>>>(grid_, grid_used_, nt); });
       timed("grid_scatter", [&] {
         k_grid_scatter<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      k_collide_integrate<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      k_collide_integrate<<<nch * COLLIDE_LANES, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
     });
     if (nre) edge(stream_, ax);
   }
@@ -746,6 +745,18 @@ int Engine::step() {
   int st;
   if (lists_dirty_ && (st = rebuild_lists()) != OK) return st;
   if ((st = upload_registry()) != OK) return st;
+  if (grid_reset_ && d_grid_) {
+    // after a failed step the bucket counts and scan words may be partial
+    B2D_CUDA(cudaMemsetAsync(d_grid_, 0, grid_head_bytes_, stream_));
+    grid_reset_ = false;
+  }
+  st = launch_step();
+  if (st != OK) grid_reset_ = true;
+  return st;
+}
+
+int Engine::launch_step() {
+  int st;
   if (profile_) return launch_all(true);
   if (!use_graph_ || plain_) return launch_all(false);
   // capture a graph once the composition has been stable for two steps;

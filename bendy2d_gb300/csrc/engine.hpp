@@ -146,6 +146,7 @@ class Engine {
   int upload_registry();
   int ensure_table(size_t n);
   int ensure_grid(size_t nbuckets, size_t np_ext);
+  int launch_step();  // eager launches or the captured graph
   int launch_all(bool profiling);
   void invalidate_graph();
   int fill_world_record(uint32_t slot);
@@ -204,6 +205,8 @@ class Engine {
   uint32_t rigid_smem_ = 0;
   uint32_t grid_used_ = 0;
   size_t grid_bytes_ = 0;
+  size_t grid_head_bytes_ = 0;  // count, range and scan words at the start of d_grid_
+  bool grid_reset_ = false;     // clear them before the next step (after a failure)
   bool lists_dirty_ = true;
   // broadphase
   DGrid grid_{};

@@ -970,12 +970,20 @@ __device__ __forceinline__ uint32_t cell_hash(int32_t cx, int32_t cy) {
   h ^= h >> 12;
   return h;
 }
+// Bucket of cell (cx, cy) in world W: four horizontally adjacent cells (a
+// strip, cx >> 2) hash together and take four consecutive buckets, so a row
+// of neighbour cells lands in one or two runs of `sorted` and its range and
+// entry loads mostly share cache lines.  (The world's bucket count is a
+// power of two >= 64, so the mask keeps the low two bits.)
+__device__ __forceinline__ uint32_t bucket_of(const DWorld& W, int32_t cx, int32_t cy) {
+  return W.gb0 + (((cell_hash(cx >> 2, cy) << 2) | ((uint32_t)cx & 3u)) & W.gmask);
+}
 
 constexpr uint32_t CHUNK = 256;  // particles per work chunk (one CTA)
 
-// Bucket entry: {pos.x bits, pos.y bits, particle index, cell x}.  An entry
-// belongs to cell (cx, cy) when its stored cell x equals cx and the cell y
-// recomputed from the stored pos.y equals cy: exact, whatever the hashing.
+// Bucket entry: {pos.x bits, pos.y bits, cell x, cell y}.  Cells that hash
+// to the same bucket are told apart by the stored cell coordinates, so the
+// neighbour search is exact whatever the hashing.
 static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __restrict__ worlds, DGrid G,
                                                       const uint2* __restrict__ chunks,
                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
@@ -986,7 +994,7 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
   const float2 p = W.pos[cur][j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
-  const uint32_t b = W.gb0 + (cell_hash(cx, cy) & W.gmask);
+  const uint32_t b = bucket_of(W, cx, cy);
   const uint32_t r = atomicAdd(&G.count[b], 1u);
   G.pbr[W.gp0 + j] = make_uint2(b, r);
 }
@@ -1020,40 +1028,109 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
   return before + x - v;
 }
 
-// sum of each SCAN_TILE counts
-static __global__ void __launch_bounds__(1024) k_scan_reduce(DGrid G, uint32_t nbuckets) {
-  const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * 4u;
-  uint32_t v = 0;
-#pragma unroll
-  for (uint32_t k = 0; k < 4; ++k)
-    if (base + k < nbuckets) v += G.count[base + k];
-  uint32_t tot;
-  block_exclusive_scan(v, &tot);
-  if (threadIdx.x == 0) G.partial[blockIdx.x] = tot;
+// Single-pass exclusive scan of the bucket counts into ranges, by decoupled
+// look-back (D. Merrill, M. Garland, "Single-pass Parallel Prefix Scan with
+// Decoupled Look-back", NVIDIA tech report NVR-2016-002).  Tiles take ids in
+// launch order from a counter; each publishes its sum, then walks back over
+// its predecessors' published words (sums, or inclusive prefixes, which end
+// the walk) and publishes its own inclusive prefix.  A tile only waits on
+// tiles with smaller ids, which had started before it, so the walk always
+// ends; it is bounded all the same and records ERR_BIT_SCAN_TIMEOUT if it
+// gives up.  Published words carry a launch epoch, so no clearing is needed
+// between launches; the last tile to finish resets the counters and advances
+// the epoch.  The scan also zeroes the counts it read, leaving them ready for
+// the next sub-step's count pass.
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long scan_word(uint32_t epoch, uint32_t kind,
+                                                        uint32_t value) {
+  return ((unsigned long long)((epoch << 2) | kind) << 32) | value;
 }
 
-// start[b] = exclusive prefix sum of count (tile offset from the partials)
-static __global__ void __launch_bounds__(1024) k_scan_apply(DGrid G, uint32_t nbuckets) {
-  __shared__ uint32_t s_off;
-  // offset of this tile: sum of the partials of the tiles before it
-  uint32_t acc = 0;
-  for (uint32_t t = threadIdx.x; t < blockIdx.x; t += blockDim.x) acc += G.partial[t];
-  uint32_t tot;
-  block_exclusive_scan(acc, &tot);
-  if (threadIdx.x == 0) s_off = tot;
-  __syncthreads();
-  const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * 4u;
-  uint32_t c[4], v = 0;
-#pragma unroll
-  for (uint32_t k = 0; k < 4; ++k) {
-    c[k] = base + k < nbuckets ? G.count[base + k] : 0u;
-    v += c[k];
+static __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets,
+                                                           uint32_t ntiles) {
+  __shared__ uint32_t s_tile, s_epoch, s_off;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(&G.tctl[0], 1u);
+    s_epoch = *reinterpret_cast<volatile uint32_t*>(&G.tctl[2]);
   }
-  uint32_t run = s_off + block_exclusive_scan(v, nullptr);
+  __syncthreads();
+  const uint32_t tile = s_tile, ep = s_epoch & 0x3FFFFFFFu;
+  // bucket ranges are whole multiples of 64, so a thread's four counts are
+  // either all inside or all outside
+  const uint32_t base = tile * SCAN_TILE + threadIdx.x * 4u;
+  uint4 c = make_uint4(0u, 0u, 0u, 0u);
+  if (base < nbuckets) {
+    uint4* cp = reinterpret_cast<uint4*>(G.count + base);
+    c = *cp;
+    *cp = make_uint4(0u, 0u, 0u, 0u);
+  }
+  uint32_t tot;
+  const uint32_t excl = block_exclusive_scan(c.x + c.y + c.z + c.w, &tot);
+  if (threadIdx.x == 0)
+    st_release_u64(&G.tstate[tile], scan_word(ep, tile == 0 ? 2u : 1u, tot));
+  if (threadIdx.x < 32u) {
+    // warp 0 looks back over windows of 32 predecessors: lane i reads tile
+    // (end - 1 - i); the window sums up to the nearest inclusive prefix
+    const uint32_t lane = threadIdx.x;
+    uint32_t off = 0;
+    int end = (int)tile;
+    const long long deadline = clock64() + WAIT_LIMIT_CYCLES;
+    bool timed_out = false;
+    while (end > 0) {
+      const int p = end - 1 - (int)lane;
+      unsigned long long w = scan_word(ep, 2u, 0u);  // before tile 0: prefix 0
+      uint32_t kind = 2u;
+      for (;;) {
+        if (p >= 0) {
+          w = ld_acquire_u64(&G.tstate[p]);
+          const uint32_t hi = (uint32_t)(w >> 32);
+          kind = (hi >> 2) == ep ? (hi & 3u) : 0u;
+        }
+        if (__all_sync(0xFFFFFFFFu, kind != 0u)) break;
+        if (__any_sync(0xFFFFFFFFu, clock64() > deadline)) {  // warp-uniform
+          timed_out = true;
+          break;
+        }
+      }
+      if (timed_out) break;
+      const uint32_t inc = __ballot_sync(0xFFFFFFFFu, kind == 2u);
+      const uint32_t stop = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest prefix
+      uint32_t v = lane <= stop ? (uint32_t)w : 0u;
 #pragma unroll
-  for (uint32_t k = 0; k < 4; ++k) {
-    if (base + k < nbuckets) G.range[base + k] = make_uint2(run, c[k]);
-    run += c[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+      off += v;
+      if (inc) break;
+      end -= 32;
+    }
+    if (lane == 0) {
+      if (timed_out) atomicOr(G.err, ERR_BIT_SCAN_TIMEOUT);
+      if (tile != 0) st_release_u64(&G.tstate[tile], scan_word(ep, 2u, off + tot));
+      s_off = off;
+    }
+  }
+  __syncthreads();
+  if (base < nbuckets) {
+    uint32_t run = s_off + excl;
+    uint4* rp = reinterpret_cast<uint4*>(G.range + base);  // two {start, count} pairs each
+    rp[0] = make_uint4(run, c.x, run + c.x, c.y);
+    run += c.x + c.y;
+    rp[1] = make_uint4(run, c.z, run + c.z, c.w);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&G.tctl[1], 1u) == ntiles - 1u) {  // last tile: reset for the next launch
+      G.tctl[0] = 0u;
+      G.tctl[1] = 0u;
+      G.tctl[2] = (s_epoch + 1u) & 0x3FFFFFFFu;
+      __threadfence();
+    }
   }
 }
 
@@ -1068,9 +1145,9 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
   if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
   const float2 p = W.pos[cur][j];
   const uint2 br = G.pbr[W.gp0 + j];
-  const int32_t cx = cell_coord(p.x, W.bx, W.cell);
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
   G.sorted[G.range[br.x].x + br.y] =
-      make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), j, (uint32_t)cx);
+      make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), (uint32_t)cx, (uint32_t)cy);
 }
 
 // Contact corrections are summed in 64-bit fixed point (units of 2^-32,
@@ -1162,16 +1239,16 @@ static __device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p)
   return p;
 }
 
-// Contacts of particle i with the particles of cell (ncx, ncy), stored in
-// bucket b.
-__device__ __forceinline__ void visit_cell(const DGrid& G, const DWorld& W, uint32_t i, float2 p,
-                                           int32_t ncx, int32_t ncy, uint32_t s0, uint32_t cnt,
-                                           float D, float D2, long long& sx, long long& sy,
-                                           bool& hit) {
+// Contacts of a particle at p with the particles of cell (ncx, ncy), whose
+// entries sit in the bucket range [s0, s0 + cnt) among those of other cells
+// that share the bucket.  The particle's own entry needs no test: it has
+// d2 = 0, which pp_contact never counts as a contact.
+__device__ __forceinline__ void visit_cell(const DGrid& G, float2 p, int32_t ncx, int32_t ncy,
+                                           uint32_t s0, uint32_t cnt, float D, float D2,
+                                           long long& sx, long long& sy, bool& hit) {
   for (uint32_t k = s0; k < s0 + cnt; ++k) {
     const uint4 e = G.sorted[k];
-    if (e.w != (uint32_t)ncx || e.z == i) continue;
-    if (cell_coord(__uint_as_float(e.y), W.by, W.cell) != ncy) continue;
+    if (e.z != (uint32_t)ncx || e.w != (uint32_t)ncy) continue;
     pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, sx, sy, hit);
   }
 }
@@ -1213,52 +1290,58 @@ __device__ __forceinline__ float4 block_box(bool act, float2 p) {
 
 // Particle collisions + bounds + integrate of one sub-step of the extension
 // pipeline.  Reads positions from buffer cur (the post-link snapshot) and
-// writes the new ones to buffer cur^1; prev is updated in place.  A CTA is
-// one chunk of one world.  Circle and polygon tests are skipped for the whole
+// writes the new ones to buffer cur^1; prev is updated in place.
+//
+// Four lanes per particle: lanes 0-2 each scan one row of the 3x3 neighbour
+// cells and the four lanes add their fixed-point sums (integer adds, so the
+// split cannot change the result); lane 0 then runs the circle and polygon
+// tests, bounds and integrate.  A CTA covers a quarter of one work chunk
+// (grid = 4 x chunks).  Circle and polygon tests are skipped for the whole
 // CTA when no circle or polygon box reaches the CTA's particles: then no
 // particle is in contact, nothing moves, and so no later test of the
 // sequence can hit either — the skip is exact.
-static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(
+constexpr uint32_t COLLIDE_LANES = 4;
+static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
     const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
-  if (blockIdx.x >= nchunks) return;
-  const uint2 ch = chunks[blockIdx.x];
+  const uint32_t cidx = blockIdx.x / COLLIDE_LANES;
+  if (cidx >= nchunks) return;
+  const uint2 ch = chunks[cidx];
   const DWorld& W = worlds[ch.x];
   if (sub >= W.S) return;  // uniform over the CTA
-  const uint32_t i = ch.y + threadIdx.x;
+  const uint32_t lane = threadIdx.x % COLLIDE_LANES;
+  const uint32_t i = ch.y + (blockIdx.x % COLLIDE_LANES) * (CHUNK / COLLIDE_LANES) +
+                     threadIdx.x / COLLIDE_LANES;
   const bool act = i < W.np;
+  const bool own = act && lane == 0;  // the lane that owns particle i
   const float2* P = W.pos[cur];
   float2 p = act ? P[i] : make_float2(0.f, 0.f);
-  float2 q = act ? W.prev[i] : make_float2(0.f, 0.f);
-  if ((W.flags & COLLIDE_PP) && act) {
-    const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
-    const float D = fadd(W.radius, W.radius);
-    const float D2 = fmul(D, D);
+  if (W.flags & COLLIDE_PP) {  // uniform over the CTA
     long long sx = 0, sy = 0;
     bool hit = false;
-    // the nine buckets' ranges are loaded together, then scanned
-#define B2D_BK(c) (W.gb0 + (cell_hash(cx + ((c) % 3) - 1, cy + ((c) / 3) - 1) & W.gmask))
-    const uint32_t b0 = B2D_BK(0), b1 = B2D_BK(1), b2 = B2D_BK(2), b3 = B2D_BK(3),
-                   b4 = B2D_BK(4), b5 = B2D_BK(5), b6 = B2D_BK(6), b7 = B2D_BK(7),
-                   b8 = B2D_BK(8);
-#undef B2D_BK
-    const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2], r3 = G.range[b3],
-                r4 = G.range[b4], r5 = G.range[b5], r6 = G.range[b6], r7 = G.range[b7],
-                r8 = G.range[b8];
-    visit_cell(G, W, i, p, cx - 1, cy - 1, r0.x, r0.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy - 1, r1.x, r1.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy - 1, r2.x, r2.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx - 1, cy, r3.x, r3.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy, r4.x, r4.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy, r5.x, r5.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx - 1, cy + 1, r6.x, r6.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx, cy + 1, r7.x, r7.y, D, D2, sx, sy, hit);
-    visit_cell(G, W, i, p, cx + 1, cy + 1, r8.x, r8.y, D, D2, sx, sy, hit);
+    if (act && lane < 3) {
+      const int32_t cx = cell_coord(p.x, W.bx, W.cell);
+      const int32_t cy = cell_coord(p.y, W.by, W.cell) + (int32_t)lane - 1;  // this lane's row
+      const float D = fadd(W.radius, W.radius);
+      const float D2 = fmul(D, D);
+      const uint32_t b0 = bucket_of(W, cx - 1, cy), b1 = bucket_of(W, cx, cy),
+                     b2 = bucket_of(W, cx + 1, cy);
+      const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2];
+      visit_cell(G, p, cx - 1, cy, r0.x, r0.y, D, D2, sx, sy, hit);
+      visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, sx, sy, hit);
+      visit_cell(G, p, cx + 1, cy, r2.x, r2.y, D, D2, sx, sy, hit);
+    }
+#pragma unroll
+    for (uint32_t o = 1; o < COLLIDE_LANES; o <<= 1) {
+      sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+      sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+      hit |= __shfl_xor_sync(0xFFFFFFFFu, (int)hit, o) != 0;
+    }
     if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
   }
   const uint32_t flags = W.flags;
   if (flags & (COLLIDE_PC | COLLIDE_PPOLY)) {
-    const float4 box = block_box(act, p);
+    const float4 box = block_box(own, p);
     bool near = false;
     if (flags & COLLIDE_PC) {
       for (uint32_t k = threadIdx.x; k < W.nc; k += blockDim.x) {
@@ -1276,14 +1359,15 @@ static __global__ void __launch_bounds__(CHUNK, 3) k_collide_integrate(
                   separated(bb.y - r, bb.w + r, box.y, box.w));
       }
     }
-    if (__syncthreads_or(near) && act) {
+    if (__syncthreads_or(near) && own) {
       if (flags & COLLIDE_PC) p = particle_circles(W, p);
       if (flags & COLLIDE_PPOLY) {
         for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
       }
     }
   }
-  if (!act) return;
+  if (!own) return;
+  float2 q = W.prev[i];
   solve_bounds(p, q, W);
   integrate(p, q, W.gx, W.gy, W.h);
   W.pos[cur ^ 1u][i] = p;

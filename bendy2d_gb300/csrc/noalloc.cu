@@ -12,7 +12,11 @@
 // that loads the library until the process exits.  Every call shares it and
 // it keeps the previous call's contents, so each call clears what must start
 // at zero; calls whose GPU work overlaps (different streams, or host threads
-// racing) corrupt each other.
+// racing) corrupt each other.  The bucket scan's control words also live
+// there and maintain themselves across calls (launch epochs); its bounded
+// wait records ERR_BIT_SCAN_TIMEOUT in a scratch word (O_ERR) that a
+// debugger can read, since this asynchronous call returns before the GPU
+// work runs.
 //
 // First call on a device: it resolves the array's device address with
 // cudaGetSymbolAddress while that device is current.  Make that first call
@@ -43,8 +47,10 @@ constexpr size_t O_WORLD = 0;
 constexpr size_t O_CHUNKS = O_WORLD + up256(sizeof(DWorld));
 constexpr size_t O_COUNT = O_CHUNKS + up256(8 * NOALLOC_MAX_CHUNKS);
 constexpr size_t O_RANGE = O_COUNT + up256(4 * NOALLOC_MAX_BUCKETS);
-constexpr size_t O_PART = O_RANGE + up256(8 * NOALLOC_MAX_BUCKETS);
-constexpr size_t O_PBR = O_PART + up256(4 * NOALLOC_MAX_TILES);
+constexpr size_t O_TSTATE = O_RANGE + up256(8 * NOALLOC_MAX_BUCKETS);
+constexpr size_t O_TCTL = O_TSTATE + up256(8 * NOALLOC_MAX_TILES);
+constexpr size_t O_ERR = O_TCTL + 256;
+constexpr size_t O_PBR = O_ERR + 256;
 constexpr size_t O_SORTED = O_PBR + up256(8 * NOALLOC_MAX_PARTICLES);
 constexpr size_t O_POS1 = O_SORTED + up256(16 * NOALLOC_MAX_PARTICLES);
 constexpr size_t NOALLOC_BYTES = O_POS1 + up256(8 * NOALLOC_MAX_PARTICLES);
@@ -135,21 +141,24 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   DGrid G;
   G.count = reinterpret_cast<uint32_t*>(base + O_COUNT);
   G.range = reinterpret_cast<uint2*>(base + O_RANGE);
-  G.partial = reinterpret_cast<uint32_t*>(base + O_PART);
+  G.tstate = reinterpret_cast<unsigned long long*>(base + O_TSTATE);
+  G.tctl = reinterpret_cast<uint32_t*>(base + O_TCTL);
+  G.err = reinterpret_cast<uint32_t*>(base + O_ERR);
   G.pbr = reinterpret_cast<uint2*>(base + O_PBR);
   G.sorted = reinterpret_cast<uint4*>(base + O_SORTED);
   G.nbuckets = nb;
 
   k_noalloc_setup<<<(nch + 255) / 256, 256, 0, st>>>(w, chunks, nch, dW);
+  // bucket counts start from zero (each scan clears what it read; this also
+  // covers a call that stopped part-way)
+  if (cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st) != cudaSuccess)
+    return fail(B2D_ERR_CUDA, "clearing the bucket counts failed");
   for (uint32_t s = 0; s < w.S; ++s) {
     const uint32_t cur = s & 1u;
-    if (cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st) != cudaSuccess)
-      return fail(B2D_ERR_CUDA, "clearing the bucket counts failed");
     k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_scan_reduce<<<nt, 1024, 0, st>>>(G, nb);
-    k_scan_apply<<<nt, 1024, 0, st>>>(G, nb);
+    k_grid_scan<<<nt, 1024, 0, st>>>(G, nb, nt);
     k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_collide_integrate<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
+    k_collide_integrate<<<nch * COLLIDE_LANES, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
   }
   k_copy_back<<<nch, CHUNK, 0, st>>>(dW, chunks, nch);
   cudaError_t e = cudaGetLastError();
