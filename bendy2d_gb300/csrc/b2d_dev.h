@@ -53,9 +53,14 @@ struct DPoly {
 // A segment is a whole level or a piece of one; a group barrier follows
 // every segment.
 constexpr uint32_t SCHED_CHUNK_WORDS = 4096;
+// shared bytes after each executor group's schedule area: two mbarriers and
+// two flag words
+constexpr uint32_t GROUP_TAIL_BYTES = 32;
 struct DSched {
   uint32_t chunk0, nchunks;  // chunk_off / chunk_len entries
   uint32_t nlvl, nops;
+  uint32_t off, words;       // the chunks are contiguous: stream[off, off + words)
+  uint32_t len0, pad;        // words of the first chunk
 };
 
 struct DWorld {

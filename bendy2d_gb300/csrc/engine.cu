@@ -61,11 +61,12 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRigidSmemCap);
     for (auto fn : {k_exec_serial_smem<true>, k_exec_serial_smem<false>})
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSerialPackBytes);
-    cudaFuncSetAttribute(k_exec_groups<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-    cudaFuncSetAttribute(k_exec_groups<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-    cudaFuncSetAttribute(k_exec_groups<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-    cudaFuncSetAttribute(k_exec_groups<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    for (auto fn : {k_exec_groups<true, true, false>, k_exec_groups<false, true, false>,
+                    k_exec_groups<true, false, false>, k_exec_groups<false, false, false>,
+                    k_exec_groups<true, true, true>, k_exec_groups<false, true, true>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   }
+  tune_.res_max = std::min<uint32_t>(tune_.res_max, (uint32_t)std::max(g_smem_optin, 48 * 1024));
   tune_.smem_max = std::min<uint32_t>(
       tune_.smem_max, (uint32_t)std::max(g_smem_optin - (int)STREAM_BYTES, 16 * 1024));
 }
@@ -416,7 +417,7 @@ int Engine::rebuild_lists() {
   size_t np_ext = 0;
   size_t nbuckets = 0, np_pp = 0;
   uint64_t rigid_smem = 0;
-  std::map<std::tuple<uint32_t, bool, bool, uint32_t>, size_t> cls;
+  std::map<std::tuple<uint32_t, bool, bool, uint32_t, uint32_t>, size_t> cls;
   wlaunch_.assign(slots_.size(), WorldLaunch());
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
@@ -428,20 +429,27 @@ int Engine::rebuild_lists() {
     wlaunch_[si].sf0 = (uint32_t)serial_full_.size();
     wlaunch_[si].pk0 = (uint32_t)packs_full_.packs.size();
     for (const GroupBody& gb : im.groups) {
-      const uint32_t rc = gb.smem ? (gb.region + 4095u) & ~4095u : 0u;
-      auto key = std::make_tuple(gb.T, gb.smem, full, rc);
+      const uint32_t rc = gb.smem ? class_region(gb.region) : 0u;
+      const uint32_t rs = gb.res ? class_res(gb.res) : 0u;
+      auto key = std::make_tuple(gb.T, gb.smem, full, rc, rs);
       auto it = cls.find(key);
       if (it == cls.end()) {
         LaunchClass c;
         c.T = gb.T;
         c.smem = gb.smem;
         c.full = full;
-        c.region = gb.smem ? std::min<uint32_t>(rc, tune_.smem_max) : 0u;
-        if (gb.smem && c.region < gb.region) c.region = gb.region;
+        c.res = rs;
+        if (rs) {
+          c.region = rc;  // the planner checked rc + rs + tail against the limit
+        } else {
+          c.region = gb.smem ? std::min<uint32_t>(rc, tune_.smem_max) : 0u;
+          if (gb.smem && c.region < gb.region) c.region = gb.region;
+        }
+        const uint32_t per_group = c.region + (rs ? rs : STREAM_BUF_BYTES) + GROUP_TAIL_BYTES;
         uint32_t G = gb.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / gb.T);
         if (gb.T != 32) G = std::min<uint32_t>(G, std::min<uint32_t>(tune_.max_groups, 15));
         G = std::max<uint32_t>(G, 1);
-        G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / (c.region + STREAM_BYTES)));
+        G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / per_group));
         c.G = G;
         it = cls.emplace(key, classes_.size()).first;
         classes_.push_back(std::move(c));
@@ -592,21 +600,26 @@ int Engine::launch_all(bool profiling) {
   const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_};
   grid_.err = d_err_;
   const DWorld* W = d_worlds_;
+  // one launch of a group class over n work items starting at L
+  auto launch_class = [&](const LaunchClass& c, const uint2* L, uint32_t n, uint32_t cur,
+                          uint32_t sub) {
+    const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
+    const uint32_t sb = c.res ? c.res : STREAM_BUF_BYTES;
+    const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
+    const uint32_t rg = c.smem ? c.region : 0u;
+    if (c.res && c.full) k_exec_groups<true, true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.res) k_exec_groups<false, true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.full && c.smem) k_exec_groups<true, true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.full) k_exec_groups<true, false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.smem) k_exec_groups<false, true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else k_exec_groups<false, false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+  };
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
       if (c.full != full || c.items.empty()) continue;
-      const uint32_t n = (uint32_t)c.items.size();
-      const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
-      const size_t sm = (size_t)c.G * (c.region + STREAM_BYTES);
-      const uint2* L = d_lists_ + c.dev_off;
       const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
                               : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
-      timed(name, [&] {
-        if (full && c.smem) k_exec_groups<true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
-        else if (full) k_exec_groups<true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
-        else if (c.smem) k_exec_groups<false, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, c.region, cur, sub);
-        else k_exec_groups<false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, 0, cur, sub);
-      });
+      timed(name, [&] { launch_class(c, d_lists_ + c.dev_off, (uint32_t)c.items.size(), cur, sub); });
     }
   };
   // Streams: link executors, grid and collide kernels run on the main
@@ -632,13 +645,8 @@ int Engine::launch_all(bool profiling) {
         const LaunchClass& lc = classes_[c];
         const uint32_t n = wl.cls[c].second;
         if (!n || !lc.full) continue;
-        const dim3 grid((n + lc.G - 1) / lc.G), block(lc.T * lc.G);
-        const size_t sm = (size_t)lc.G * (lc.region + STREAM_BYTES);
         const uint2* L = d_lists_ + lc.dev_off + wl.cls[c].first;
-        timed("plain_exec_groups", [&] {
-          if (lc.smem) k_exec_groups<true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, lc.T, lc.G, lc.region, 0, 0);
-          else k_exec_groups<true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, lc.T, lc.G, 0, 0, 0);
-        });
+        timed("plain_exec_groups", [&] { launch_class(lc, L, n, 0, 0); });
       }
       if (wl.pkn) {
         const SerialPacks& P = packs_full_;

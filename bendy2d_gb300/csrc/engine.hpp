@@ -27,6 +27,8 @@ struct PlanTuning {
   uint32_t warp_groups = 8;         // groups per CTA when T == 32
   uint32_t max_groups = 15;         // groups per CTA when T > 32
   float width_per_thread = 0.5f;    // T = pow2 >= avg width / this (issue-bound: wide groups win)
+  uint32_t resident = 1;            // load a body's whole schedule when it fits
+  uint32_t res_max = 227 * 1024;    // shared bytes per group for body + resident schedule
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };
@@ -44,8 +46,15 @@ struct GroupBody {
   uint32_t body;
   uint32_t T;
   uint32_t region;  // shared bytes for this body (0 when run from global memory)
+  uint32_t res;     // bytes of its schedule when held whole in shared memory, else 0
   bool smem;
 };
+
+// Launch classes round their members' shared-memory needs up to these steps
+// (body region, resident schedule); the planner applies the same rounding
+// when it decides whether a schedule fits.
+inline uint32_t class_region(uint32_t r) { return (r + 4095u) & ~4095u; }
+inline uint32_t class_res(uint32_t r) { return (r + 8191u) & ~8191u; }
 
 struct PlanStats {
   uint32_t bodies = 0, group_bodies = 0, serial_bodies = 0, global_bodies = 0;
@@ -94,6 +103,7 @@ void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst)
 
 struct LaunchClass {
   uint32_t T, G, region;
+  uint32_t res;  // resident schedule bytes per group (0: streamed in chunks)
   bool smem, full;
   std::vector<uint2> items;
   size_t dev_off = 0;  // offset (in uint2) into the device list buffer

@@ -92,6 +92,8 @@ __device__ __forceinline__ void integrate(float2& p, float2& q, float ax, float 
 __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
   if (T == 32) {
     __syncwarp();
+  } else if (T == blockDim.x) {
+    __syncthreads();  // one group per CTA: the plain barrier measured ~5% faster per level
   } else {
     asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(T) : "memory");
   }
@@ -148,9 +150,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return true;
 }
 
-// shared bytes per group beyond the body region: two chunk buffers, two
-// mbarriers and a broadcast word
-constexpr uint32_t STREAM_BYTES = 2 * SCHED_CHUNK_WORDS * 4 + 32;
+// shared bytes per group beyond the body region when the schedule streams:
+// two chunk buffers, then two mbarriers and two flag words (GROUP_TAIL_BYTES)
+constexpr uint32_t STREAM_BUF_BYTES = 2 * SCHED_CHUNK_WORDS * 4;
+constexpr uint32_t STREAM_BYTES = STREAM_BUF_BYTES + 32;
 
 // ----------------------------------------------------------------------------
 // Body executor (block / warp granularity).
@@ -190,10 +193,11 @@ __device__ __forceinline__ void sts_f32x2(uint32_t a, float2 v) {
   asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
 }
 
-template <bool FULL, bool SMEM>
+template <bool FULL, bool SMEM, bool RES>
 __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
-                              uint32_t G, uint32_t region_bytes, uint32_t cur, uint32_t sub) {
+                              uint32_t G, uint32_t region_bytes, uint32_t sched_bytes,
+                              uint32_t cur, uint32_t sub) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
   const uint32_t item = blockIdx.x * G + g;
@@ -213,16 +217,17 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   DWorld Wb;  // bounds only
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
 
-  unsigned char* base = smem + (size_t)g * (region_bytes + STREAM_BYTES);
+  // per group: body region | schedule area (sched_bytes: the whole schedule
+  // when RES, else two chunk buffers) | two mbarriers and two flag words
+  unsigned char* base = smem + (size_t)g * (region_bytes + sched_bytes + GROUP_TAIL_BYTES);
   uint32_t* cbuf = reinterpret_cast<uint32_t*>(base + region_bytes);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(cbuf + 2 * SCHED_CHUNK_WORDS);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + region_bytes + sched_bytes);
   volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(bar + 2);
   if (t == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
-    if (S.nchunks > 0)
-      bulk_load(cbuf, SC.stream + SC.chunk_off[S.chunk0], SC.chunk_len[S.chunk0] * 4u, &bar[0]);
+    if (S.nchunks > 0) bulk_load(cbuf, SC.stream + S.off, (RES ? S.words : S.len0) * 4u, &bar[0]);
   }
   // body state in shared memory: pos[np], prev[np] (FULL), {rest, stiff}[nl]
   const uint32_t sp_a = smem_addr(base);
@@ -242,85 +247,107 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 #pragma unroll 4
     for (uint32_t i = t; i < B.nl; i += T) srs[i] = make_float2(grest[i], gstiff[i]);
   }
+  // a resident schedule is waited for once, under the same barrier
+  if (RES && t == 0 && S.nchunks > 0) flag[0] = mbar_wait_bounded(&bar[0], 0u) ? 1u : 0u;
   group_sync(g, T);
-
-  const uint32_t cbuf_a = smem_addr(cbuf);
-  // buffer k2 = c & 1 is used for the (c >> 1)-th time: its mbarrier phase
-  // parity is (c >> 1) & 1
-  for (uint32_t c = 0; c < S.nchunks; ++c) {
-    const uint32_t k2 = c & 1u;
-    const uint32_t par = (c >> 1) & 1u;
-    if (t == 0) *flag = mbar_wait_bounded(&bar[k2], par) ? 1u : 0u;
-    group_sync(g, T);
-    if (*flag == 0u) {
+  if (RES && S.nchunks > 0) {
+    if (flag[0] == 0u) {
       if (t == 0) {
         atomicOr(SC.err, ERR_BIT_TMA_TIMEOUT);
-        mbar_wait_bounded(&bar[k2], par);  // let the copy in flight land
+        mbar_wait_bounded(&bar[0], 0u);  // let the copy in flight land
       }
       return;  // every thread of the group leaves together
     }
-    mbar_try(&bar[k2], par);  // completed phase: makes the data visible here
-    if (t == 0 && c + 1 < S.nchunks) {
-      fence_proxy_async();
-      bulk_load(cbuf + (k2 ^ 1u) * SCHED_CHUNK_WORDS, SC.stream + SC.chunk_off[S.chunk0 + c + 1],
-                SC.chunk_len[S.chunk0 + c + 1] * 4u, &bar[k2 ^ 1u]);
+    mbar_try(&bar[0], 0u);  // completed phase: makes the data visible here
+  }
+
+  // One op: a link solve or (FULL) bounds + integrate of one particle.
+  auto run = [&](uint2 op) {
+    if (FULL && op.y == OP_INTEG) {
+      float2 p, q;
+      if (SMEM) {
+        p = lds_f32x2(sp_a + 8u * op.x);
+        q = lds_f32x2(sq_a + 8u * op.x);
+      } else {
+        p = gp[bidx[op.x]];
+        q = gq[bidx[op.x]];
+      }
+      solve_bounds(p, q, Wb);
+      integrate(p, q, gx, gy, h);
+      if (SMEM) {
+        sts_f32x2(sp_a + 8u * op.x, p);
+        sts_f32x2(sq_a + 8u * op.x, q);
+      } else {
+        gp[bidx[op.x]] = p;
+        gq[bidx[op.x]] = q;
+      }
+    } else if (SMEM) {
+      const float2 rs = lds_f32x2(srs_a + 8u * op.y);
+      const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
+      float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
+      link_solve(pa, pb, rs.x, rs.y);
+      sts_f32x2(aa, pa);
+      sts_f32x2(ba, pb);
+    } else {
+      uint32_t ia, ib, kl;
+      if (op.y == OP_WIDE) {
+        kl = op.x;
+        ia = gab[kl].x;
+        ib = gab[kl].y;
+      } else {
+        kl = op.y;
+        ia = bidx[op.x & 0xFFFFu];
+        ib = bidx[op.x >> 16];
+      }
+      float2 pa = gp[ia], pb = gp[ib];
+      link_solve(pa, pb, grest[kl], gstiff[kl]);
+      gp[ia] = pa;
+      gp[ib] = pb;
     }
-    const uint32_t buf_a = cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u;
+  };
+  // One chunk at shared address buf_a: its segments in order, each followed
+  // by the group barrier; a segment's ops go to the group's threads in turn.
+  // (Prefetching the next segment's op ahead of the barrier measured slower
+  // than this plain form.)  Returns the address just past the chunk.
+  auto run_chunk = [&](uint32_t buf_a) {
     const uint32_t nseg = lds_u32(buf_a);
     const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
-    // One op: a link solve or (FULL) bounds + integrate of one particle.
-    auto run = [&](uint2 op) {
-      if (FULL && op.y == OP_INTEG) {
-        float2 p, q;
-        if (SMEM) {
-          p = lds_f32x2(sp_a + 8u * op.x);
-          q = lds_f32x2(sq_a + 8u * op.x);
-        } else {
-          p = gp[bidx[op.x]];
-          q = gq[bidx[op.x]];
-        }
-        solve_bounds(p, q, Wb);
-        integrate(p, q, gx, gy, h);
-        if (SMEM) {
-          sts_f32x2(sp_a + 8u * op.x, p);
-          sts_f32x2(sq_a + 8u * op.x, q);
-        } else {
-          gp[bidx[op.x]] = p;
-          gq[bidx[op.x]] = q;
-        }
-      } else if (SMEM) {
-        const float2 rs = lds_f32x2(srs_a + 8u * op.y);
-        const uint32_t aa = sp_a + 8u * (op.x & 0xFFFFu), ba = sp_a + 8u * (op.x >> 16);
-        float2 pa = lds_f32x2(aa), pb = lds_f32x2(ba);
-        link_solve(pa, pb, rs.x, rs.y);
-        sts_f32x2(aa, pa);
-        sts_f32x2(ba, pb);
-      } else {
-        uint32_t ia, ib, kl;
-        if (op.y == OP_WIDE) {
-          kl = op.x;
-          ia = gab[kl].x;
-          ib = gab[kl].y;
-        } else {
-          kl = op.y;
-          ia = bidx[op.x & 0xFFFFu];
-          ib = bidx[op.x >> 16];
-        }
-        float2 pa = gp[ia], pb = gp[ib];
-        link_solve(pa, pb, grest[kl], gstiff[kl]);
-        gp[ia] = pa;
-        gp[ib] = pb;
-      }
-    };
-    // Segment loop: the segment's ops go to the group's threads in turn,
-    // then the group barrier.  (Prefetching the next segment's op ahead of
-    // the barrier measured slower than this plain form.)
     uint32_t beg = 0;
     for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
       const uint32_t end = lds_u32(buf_a + 4u + 4u * sgi);
       for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
       group_sync(g, T);
       beg = end;
+    }
+    return (ops_a + 8u * beg + 15u) & ~15u;  // chunks are padded to 16 bytes
+  };
+
+  const uint32_t cbuf_a = smem_addr(cbuf);
+  if (RES) {
+    uint32_t buf_a = cbuf_a;
+    for (uint32_t c = 0; c < S.nchunks; ++c) buf_a = run_chunk(buf_a);
+  } else {
+    // buffer k2 = c & 1 is used for the (c >> 1)-th time: its mbarrier
+    // phase parity is (c >> 1) & 1
+    for (uint32_t c = 0; c < S.nchunks; ++c) {
+      const uint32_t k2 = c & 1u;
+      const uint32_t par = (c >> 1) & 1u;
+      if (t == 0) flag[0] = mbar_wait_bounded(&bar[k2], par) ? 1u : 0u;
+      group_sync(g, T);
+      if (flag[0] == 0u) {
+        if (t == 0) {
+          atomicOr(SC.err, ERR_BIT_TMA_TIMEOUT);
+          mbar_wait_bounded(&bar[k2], par);  // let the copy in flight land
+        }
+        return;  // every thread of the group leaves together
+      }
+      mbar_try(&bar[k2], par);  // completed phase: makes the data visible here
+      if (t == 0 && c + 1 < S.nchunks) {
+        fence_proxy_async();
+        bulk_load(cbuf + (k2 ^ 1u) * SCHED_CHUNK_WORDS, SC.stream + SC.chunk_off[S.chunk0 + c + 1],
+                  SC.chunk_len[S.chunk0 + c + 1] * 4u, &bar[k2 ^ 1u]);
+      }
+      run_chunk(cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u);
     }
   }
 

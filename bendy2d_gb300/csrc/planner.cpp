@@ -38,6 +38,8 @@ bool PlanTuning::set(const std::string& k, double v) {
   else if (k == "warp_groups") warp_groups = (uint32_t)v;
   else if (k == "max_groups") max_groups = (uint32_t)v;
   else if (k == "width_per_thread") width_per_thread = (float)v;
+  else if (k == "resident") resident = (uint32_t)v;
+  else if (k == "res_max") res_max = (uint32_t)v;
   else return false;
   return true;
 }
@@ -146,6 +148,14 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   }
   flush();
   d.nchunks = (uint32_t)chunk_off.size() - d.chunk0;
+  d.off = d.words = d.len0 = d.pad = 0;
+  if (d.nchunks) {
+    d.off = chunk_off[d.chunk0];
+    d.len0 = chunk_len[d.chunk0];
+    for (uint32_t c = d.chunk0; c + 1 < d.chunk0 + d.nchunks; ++c)  // self-check: contiguous
+      if (chunk_off[c] + chunk_len[c] != chunk_off[c + 1]) std::abort();
+    d.words = chunk_off.back() + chunk_len.back() - d.off;
+  }
   const uint32_t id = (uint32_t)scheds.size();
   scheds.push_back(d);
   index.emplace(std::move(key), id);
@@ -182,8 +192,11 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
     const DBody& B = im.bodies[g.body];
     if (B.sched >= reg.scheds.size()) return bad("schedule id");
     const DSched& S = reg.scheds[B.sched];
-    if ((size_t)S.chunk0 + S.nchunks > reg.chunk_off.size()) return bad("schedule range");
+    if ((size_t)S.chunk0 + S.nchunks > reg.chunk_off.size() ||
+        (size_t)S.off + S.words > reg.stream.size())
+      return bad("schedule range");
     if (g.smem && (!B.local || B.np > 65535u)) return bad("shared-memory body needs local links");
+    if (g.res && (!g.smem || g.res != S.words * 4u)) return bad("resident schedule size");
     if (g.T < 32 || g.T % 32) return bad("group size");
   }
   for (uint32_t b : im.serials)
@@ -342,6 +355,14 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
     T = std::min(std::max(T, tune.t_min), tune.t_max);
     const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 8u * (size_t)B.nl);
     const bool smem = region <= tune.smem_max && B.np <= 65535u;
+    // the whole schedule resident in shared memory when it fits beside the body
+    uint32_t res = 0;
+    if (smem && tune.resident) {
+      const size_t sb = (size_t)S.words * 4u;
+      if ((size_t)class_region((uint32_t)region) + class_res((uint32_t)sb) + GROUP_TAIL_BYTES <=
+          tune.res_max)
+        res = (uint32_t)sb;
+    }
     B.local = smem ? 1u : 0u;
     for (size_t i = 0; i < loc.size(); ++i) {
       if (smem) im.lab.push_back(loc[i]);
@@ -349,7 +370,7 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
     }
     const uint32_t id = (uint32_t)im.bodies.size();
     im.bodies.push_back(B);
-    im.groups.push_back(GroupBody{id, T, smem ? (uint32_t)region : 0u, smem});
+    im.groups.push_back(GroupBody{id, T, smem ? (uint32_t)region : 0u, res, smem});
     im.stats.group_bodies++;
     if (!smem) im.stats.global_bodies++;
     im.stats.levels += S.nlvl;

@@ -298,6 +298,22 @@ def test_graph_and_eager_launches_agree(gpu):
     assert_same_state(solver_state(a), solver_state(b), "graph vs eager")
 
 
+@pytest.mark.parametrize("full", [False, True])
+def test_resident_and_streamed_schedules_agree(gpu, full):
+    """A body's schedule is either held whole in shared memory (one bulk
+    copy) or streamed through two chunk buffers; both run the same ops."""
+    from bendy2d_gb300 import scenes
+    collide = 7 if not full else 0
+    sc = scenes.config2(seed=8, n_bodies=3, box=120.0, n_circles=2, n_polys=1, collide=collide)
+    b = sc.to_solver()
+    b.set_tuning(resident=0)
+    a, o = run_both(sc, 3)
+    for _ in range(3):
+        b.update(sc.dt)
+    assert_same_state(solver_state(a), solver_state(b), "resident vs streamed")
+    assert_same_state(solver_state(a), oracle_state(o), "resident vs oracle")
+
+
 def test_config5_full_size_isolated_bodies_match_oracle(gpu):
     """Full configuration 5 (1,048,576 particles, fast mode, collisions) for
     one step on the GPU.  Size-independent check: bodies are 90 units apart,
