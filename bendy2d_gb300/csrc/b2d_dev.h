@@ -31,7 +31,10 @@ struct DBody {
   uint32_t l0, nl;       // links lab[l0 .. l0+nl) in insertion order
   uint32_t sched;        // schedule id (group executors), else unused
   uint32_t local;        // 1: link endpoints are body-local; 0: world indices
+  uint32_t first;        // bidx[i0 + i] == first + i for every i, else NO_FIRST
+  uint32_t pad;
 };
+constexpr uint32_t NO_FIRST = 0xFFFFFFFFu;
 
 struct DPoly {
   uint32_t v0, nv;       // vertices
@@ -112,7 +115,8 @@ enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_SCAN_TIMEOUT = 2u };
 // Extension broadphase: hashed uniform grid built by a counting sort each
 // sub-step.  Every world with particle collisions owns a power-of-two range
 // of buckets; a bucket's entries are contiguous in `sorted`.
-constexpr uint32_t SCAN_TILE = 4096;  // buckets per scan block (1024 threads x 4)
+constexpr uint32_t SCAN_SUB = 4096;  // buckets per scan sub-tile (1024 threads x 4); a
+                                     // tile is 1 or 4 sub-tiles
 struct DGrid {
   uint32_t* count;       // nbuckets: entries per bucket (all zero between sub-steps)
   uint2* range;          // nbuckets: {exclusive prefix sum of count, count}

@@ -49,6 +49,7 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     own_stream_ = true;
   }
   for (auto& a : aux_) cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
+  for (auto& a : lx_) cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
   evpool_.resize(256);
   for (auto& e : evpool_) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   if (g_smem_optin < 0) {
@@ -87,6 +88,7 @@ Engine::~Engine() {
   cudaFree(d_grid_);
   for (auto& e : evpool_) cudaEventDestroy(e);
   for (auto& a : aux_) cudaStreamDestroy(a);
+  for (auto& a : lx_) cudaStreamDestroy(a);
   if (own_stream_) cudaStreamDestroy(stream_);
 }
 
@@ -333,7 +335,7 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   if (nbuckets <= grid_.nbuckets && np_pp <= grid_np_ && d_grid_) return OK;
   const size_t nb = std::max(nbuckets, (size_t)grid_.nbuckets);
   const size_t np = std::max<size_t>(std::max(np_pp, grid_np_), 1);
-  const size_t ntiles = (nb + SCAN_TILE - 1) / SCAN_TILE;
+  const size_t ntiles = (nb + SCAN_SUB - 1) / SCAN_SUB;  // most tiles: one sub-tile each
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
   const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_tstate = seg(ntiles * 8),
@@ -418,6 +420,16 @@ int Engine::rebuild_lists() {
   size_t nbuckets = 0, np_pp = 0;
   uint64_t rigid_smem = 0;
   std::map<std::tuple<uint32_t, bool, bool, uint32_t, uint32_t>, size_t> cls;
+  // A resident schedule takes most of an SM's shared memory (a 32x32 cloth:
+  // ~170 KB, one body per SM) where a streamed one leaves room for about
+  // three.  Resident schedules win when a launch has no more bodies than SMs
+  // (each body's level chain is the critical path); larger launches are
+  // throughput-bound and stream.
+  std::map<std::tuple<uint32_t, bool, uint32_t>, size_t> res_count;
+  for (const Slot& s : slots_)
+    if (s.live)
+      for (const GroupBody& gb : s.img.groups)
+        if (gb.res) ++res_count[std::make_tuple(gb.T, !s.img.ext, class_region(gb.region))];
   wlaunch_.assign(slots_.size(), WorldLaunch());
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
@@ -430,7 +442,9 @@ int Engine::rebuild_lists() {
     wlaunch_[si].pk0 = (uint32_t)packs_full_.packs.size();
     for (const GroupBody& gb : im.groups) {
       const uint32_t rc = gb.smem ? class_region(gb.region) : 0u;
-      const uint32_t rs = gb.res ? class_res(gb.res) : 0u;
+      const bool use_res =
+          gb.res && res_count[std::make_tuple(gb.T, full, rc)] <= (size_t)std::max(g_num_sms, 1);
+      const uint32_t rs = use_res ? class_res(gb.res) : 0u;
       auto key = std::make_tuple(gb.T, gb.smem, full, rc, rs);
       auto it = cls.find(key);
       if (it == cls.end()) {
@@ -600,28 +614,6 @@ int Engine::launch_all(bool profiling) {
   const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_};
   grid_.err = d_err_;
   const DWorld* W = d_worlds_;
-  // one launch of a group class over n work items starting at L
-  auto launch_class = [&](const LaunchClass& c, const uint2* L, uint32_t n, uint32_t cur,
-                          uint32_t sub) {
-    const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
-    const uint32_t sb = c.res ? c.res : STREAM_BUF_BYTES;
-    const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
-    const uint32_t rg = c.smem ? c.region : 0u;
-    if (c.res && c.full) k_exec_groups<true, true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.res) k_exec_groups<false, true, true><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.full && c.smem) k_exec_groups<true, true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.full) k_exec_groups<true, false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.smem) k_exec_groups<false, true, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else k_exec_groups<false, false, false><<<grid, block, sm, stream_>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-  };
-  auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
-    for (const LaunchClass& c : classes_) {
-      if (c.full != full || c.items.empty()) continue;
-      const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
-                              : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
-      timed(name, [&] { launch_class(c, d_lists_ + c.dev_off, (uint32_t)c.items.size(), cur, sub); });
-    }
-  };
   // Streams: link executors, grid and collide kernels run on the main
   // stream; circle/polygon kernels on aux streams (graph branches), joined
   // before the collide kernel that reads them.  Profiling runs serially.
@@ -633,6 +625,56 @@ int Engine::launch_all(bool profiling) {
     cudaEvent_t e = evpool_[evi++ % evpool_.size()];
     cudaEventRecord(e, a);
     cudaStreamWaitEvent(b, e, 0);
+  };
+  // Link-phase launches of one pass (group classes, serial packs, serial
+  // bodies) touch disjoint bodies, so they run side by side: the first on the
+  // main stream, the others on branch streams forked from one event recorded
+  // before the pass, and all joined back before the grid and collide kernels.
+  uint32_t br_used = 0, br_next = 0;
+  cudaEvent_t fork_ev = nullptr;
+  auto begin_pass = [&]() {
+    br_used = br_next = 0;
+    if (profiling) return;
+    fork_ev = evpool_[evi++ % evpool_.size()];
+    cudaEventRecord(fork_ev, stream_);
+  };
+  auto branch = [&]() -> cudaStream_t {
+    const uint32_t i = br_next++;
+    if (profiling || i == 0) return stream_;
+    const uint32_t k = (i - 1) % kLinkBranches;
+    if (!(br_used & (1u << k))) {
+      cudaStreamWaitEvent(lx_[k], fork_ev, 0);
+      br_used |= 1u << k;
+    }
+    return lx_[k];
+  };
+  auto end_pass = [&]() {
+    for (uint32_t k = 0; k < kLinkBranches; ++k)
+      if (br_used & (1u << k)) edge(lx_[k], stream_);
+    br_used = br_next = 0;
+  };
+  // one launch of a group class over n work items starting at L
+  auto launch_class = [&](const LaunchClass& c, const uint2* L, uint32_t n, uint32_t cur,
+                          uint32_t sub, cudaStream_t st) {
+    const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
+    const uint32_t sb = c.res ? c.res : STREAM_BUF_BYTES;
+    const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
+    const uint32_t rg = c.smem ? c.region : 0u;
+    if (c.res && c.full) k_exec_groups<true, true, true><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.res) k_exec_groups<false, true, true><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.full && c.smem) k_exec_groups<true, true, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.full) k_exec_groups<true, false, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else if (c.smem) k_exec_groups<false, true, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    else k_exec_groups<false, false, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+  };
+  auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
+    for (const LaunchClass& c : classes_) {
+      if (c.full != full || c.items.empty()) continue;
+      const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
+                              : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
+      const cudaStream_t st = branch();
+      timed(name, [&] { launch_class(c, d_lists_ + c.dev_off, (uint32_t)c.items.size(), cur, sub, st); });
+    }
   };
   edge(stream_, ax);
   edge(stream_, ax2);
@@ -646,7 +688,7 @@ int Engine::launch_all(bool profiling) {
         const uint32_t n = wl.cls[c].second;
         if (!n || !lc.full) continue;
         const uint2* L = d_lists_ + lc.dev_off + wl.cls[c].first;
-        timed("plain_exec_groups", [&] { launch_class(lc, L, n, 0, 0); });
+        timed("plain_exec_groups", [&] { launch_class(lc, L, n, 0, 0, stream_); });
       }
       if (wl.pkn) {
         const SerialPacks& P = packs_full_;
@@ -670,21 +712,25 @@ int Engine::launch_all(bool profiling) {
     }
   } else {
   // worlds without extension collisions: one launch per class for the whole step
+  begin_pass();
   groups(true, 0, 0);
   if (!packs_full_.packs.empty()) {
     const SerialPacks& P = packs_full_;
     const uint32_t n = (uint32_t)P.packs.size();
+    const cudaStream_t st = branch();
     timed("exec_serial_smem_full", [&] {
-      k_exec_serial_smem<true><<<n, kSerialPackThreads, P.max_bytes, stream_>>>(
+      k_exec_serial_smem<true><<<n, kSerialPackThreads, P.max_bytes, st>>>(
           W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, 0, 0);
     });
   }
   if (!serial_full_.empty()) {
     const uint32_t n = (uint32_t)serial_full_.size();
+    const cudaStream_t st = branch();
     timed("exec_serial_full", [&] {
-      k_exec_serial<true><<<(n + 127) / 128, 128, 0, stream_>>>(W, d_lists_ + off_serial_full_, n, 0, 0);
+      k_exec_serial<true><<<(n + 127) / 128, 128, 0, st>>>(W, d_lists_ + off_serial_full_, n, 0, 0);
     });
   }
+  end_pass();
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
     timed("rigid_full", [&] { k_rigid<0><<<n, 256, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
@@ -703,28 +749,41 @@ int Engine::launch_all(bool profiling) {
         else k_rigid<3><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
       });
     }
+    begin_pass();
     groups(false, cur, s);
     if (!packs_links_.packs.empty()) {
       const SerialPacks& P = packs_links_;
       const uint32_t n = (uint32_t)P.packs.size();
+      const cudaStream_t st = branch();
       timed("exec_serial_smem_links", [&] {
-        k_exec_serial_smem<false><<<n, kSerialPackThreads, P.max_bytes, stream_>>>(
+        k_exec_serial_smem<false><<<n, kSerialPackThreads, P.max_bytes, st>>>(
             W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, cur, s);
       });
     }
     if (!serial_links_.empty()) {
       const uint32_t n = (uint32_t)serial_links_.size();
+      const cudaStream_t st = branch();
       timed("exec_serial_links", [&] {
-        k_exec_serial<false><<<(n + 127) / 128, 128, 0, stream_>>>(W, d_lists_ + off_serial_links_, n, cur, s);
+        k_exec_serial<false><<<(n + 127) / 128, 128, 0, st>>>(W, d_lists_ + off_serial_links_, n, cur, s);
       });
     }
+    end_pass();
     if (any_pp_) {
       // counts are all zero here: the scan of the previous sub-step cleared them
-      const uint32_t nt = (grid_used_ + SCAN_TILE - 1) / SCAN_TILE;
+      // tiles of one sub-tile while that gives at most two per SM, else four
+      const uint32_t nsub = (grid_used_ + SCAN_SUB - 1) / SCAN_SUB;
+      const uint32_t subs = nsub <= 2u * (uint32_t)std::max(g_num_sms, 1) ? 1u : 4u;
+      const uint32_t nt = (nsub + subs - 1) / subs;
       timed("grid_count", [&] {
         k_grid_count<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });
-      timed("grid_scan", [&] { k_grid_scan<<<nt, 1024, 0, stream_>>>(grid_, grid_used_, nt); });
+      // one-sub-tile CTAs fit two per SM, four-sub-tile ones one per SM
+      const uint32_t ncta =
+          std::min<uint32_t>(nt, (subs == 1 ? 2u : 1u) * (uint32_t)std::max(g_num_sms, 1));
+      timed("grid_scan", [&] {
+        if (subs == 1) k_grid_scan<1><<<ncta, 1024, 0, stream_>>>(grid_, grid_used_, nt);
+        else k_grid_scan<4><<<ncta, 1024, 0, stream_>>>(grid_, grid_used_, nt);
+      });
       timed("grid_scatter", [&] {
         k_grid_scatter<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
       });

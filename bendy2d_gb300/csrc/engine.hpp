@@ -164,6 +164,8 @@ class Engine {
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   cudaStream_t aux_[2] = {nullptr, nullptr};  // graph branches (circles/polygons)
+  static constexpr uint32_t kLinkBranches = 3;
+  cudaStream_t lx_[kLinkBranches] = {};       // graph branches of the link phase
   std::vector<struct CUevent_st*> evpool_;
   PlanTuning tune_;
   SchedRegistry reg_;

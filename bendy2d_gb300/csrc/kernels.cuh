@@ -234,18 +234,22 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   const uint32_t sq_a = sp_a + 8u * B.np;
   const uint32_t srs_a = sq_a + (FULL ? 8u * B.np : 0u);
   if (SMEM) {
-    // plain stores here, so the compiler can keep many global loads in flight
+    // One pass issues the particle and link-parameter loads together (plain
+    // stores, so the compiler keeps many global loads in flight); a body
+    // whose particles are contiguous in the world skips the bidx indirection.
     float2* sp = reinterpret_cast<float2*>(base);
     float2* sq = sp + B.np;
     float2* srs = sq + (FULL ? B.np : 0u);
+    const uint32_t n = B.np > B.nl ? B.np : B.nl;
 #pragma unroll 4
-    for (uint32_t i = t; i < B.np; i += T) {
-      const uint32_t k = bidx[i];
-      sp[i] = gp[k];
-      if (FULL) sq[i] = gq[k];
+    for (uint32_t i = t; i < n; i += T) {
+      if (i < B.np) {
+        const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
+        sp[i] = gp[k];
+        if (FULL) sq[i] = gq[k];
+      }
+      if (i < B.nl) srs[i] = make_float2(grest[i], gstiff[i]);
     }
-#pragma unroll 4
-    for (uint32_t i = t; i < B.nl; i += T) srs[i] = make_float2(grest[i], gstiff[i]);
   }
   // a resident schedule is waited for once, under the same barrier
   if (RES && t == 0 && S.nchunks > 0) flag[0] = mbar_wait_bounded(&bar[0], 0u) ? 1u : 0u;
@@ -356,7 +360,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     const float2* sq = sp + B.np;
 #pragma unroll 4
     for (uint32_t i = t; i < B.np; i += T) {
-      const uint32_t k = bidx[i];
+      const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
       gp[k] = sp[i];
       if (FULL) gq[k] = sq[i];
     }
@@ -1057,16 +1061,17 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 // Single-pass exclusive scan of the bucket counts into ranges, by decoupled
 // look-back (D. Merrill, M. Garland, "Single-pass Parallel Prefix Scan with
-// Decoupled Look-back", NVIDIA tech report NVR-2016-002).  Tiles take ids in
-// launch order from a counter; each publishes its sum, then walks back over
-// its predecessors' published words (sums, or inclusive prefixes, which end
-// the walk) and publishes its own inclusive prefix.  A tile only waits on
-// tiles with smaller ids, which had started before it, so the walk always
-// ends; it is bounded all the same and records ERR_BIT_SCAN_TIMEOUT if it
-// gives up.  Published words carry a launch epoch, so no clearing is needed
-// between launches; the last tile to finish resets the counters and advances
-// the epoch.  The scan also zeroes the counts it read, leaving them ready for
-// the next sub-step's count pass.
+// Decoupled Look-back", NVIDIA tech report NVR-2016-002).  Persistent CTAs
+// take tile ids in order from a counter; each tile publishes its sum, then
+// walks back over its predecessors' published words (sums, or inclusive
+// prefixes, which end the walk) and publishes its own inclusive prefix.  A
+// tile only waits on tiles with smaller ids, which running CTAs had already
+// taken and publish without waiting, so the walk always ends; it is bounded
+// all the same and records ERR_BIT_SCAN_TIMEOUT if it gives up.  Published
+// words carry a launch epoch, so no clearing is needed between launches; the
+// last CTA to finish resets the counters and advances the epoch.  The scan
+// also zeroes the counts it read, leaving them ready for the next sub-step's
+// count pass.
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -1080,79 +1085,137 @@ __device__ __forceinline__ unsigned long long scan_word(uint32_t epoch, uint32_t
   return ((unsigned long long)((epoch << 2) | kind) << 32) | value;
 }
 
-static __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets,
-                                                           uint32_t ntiles) {
-  __shared__ uint32_t s_tile, s_epoch, s_off;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(&G.tctl[0], 1u);
-    s_epoch = *reinterpret_cast<volatile uint32_t*>(&G.tctl[2]);
-  }
-  __syncthreads();
-  const uint32_t tile = s_tile, ep = s_epoch & 0x3FFFFFFFu;
-  // bucket ranges are whole multiples of 64, so a thread's four counts are
-  // either all inside or all outside
-  const uint32_t base = tile * SCAN_TILE + threadIdx.x * 4u;
-  uint4 c = make_uint4(0u, 0u, 0u, 0u);
-  if (base < nbuckets) {
-    uint4* cp = reinterpret_cast<uint4*>(G.count + base);
-    c = *cp;
-    *cp = make_uint4(0u, 0u, 0u, 0u);
-  }
-  uint32_t tot;
-  const uint32_t excl = block_exclusive_scan(c.x + c.y + c.z + c.w, &tot);
-  if (threadIdx.x == 0)
-    st_release_u64(&G.tstate[tile], scan_word(ep, tile == 0 ? 2u : 1u, tot));
-  if (threadIdx.x < 32u) {
-    // warp 0 looks back over windows of 32 predecessors: lane i reads tile
-    // (end - 1 - i); the window sums up to the nearest inclusive prefix
-    const uint32_t lane = threadIdx.x;
-    uint32_t off = 0;
-    int end = (int)tile;
-    const long long deadline = clock64() + WAIT_LIMIT_CYCLES;
-    bool timed_out = false;
-    while (end > 0) {
-      const int p = end - 1 - (int)lane;
-      unsigned long long w = scan_word(ep, 2u, 0u);  // before tile 0: prefix 0
-      uint32_t kind = 2u;
-      for (;;) {
-        if (p >= 0) {
-          w = ld_acquire_u64(&G.tstate[p]);
-          const uint32_t hi = (uint32_t)(w >> 32);
-          kind = (hi >> 2) == ep ? (hi & 3u) : 0u;
-        }
-        if (__all_sync(0xFFFFFFFFu, kind != 0u)) break;
-        if (__any_sync(0xFFFFFFFFu, clock64() > deadline)) {  // warp-uniform
-          timed_out = true;
-          break;
-        }
-      }
-      if (timed_out) break;
-      const uint32_t inc = __ballot_sync(0xFFFFFFFFu, kind == 2u);
-      const uint32_t stop = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest prefix
-      uint32_t v = lane <= stop ? (uint32_t)w : 0u;
+// block-wide exclusive scan of four values per thread at once (blockDim =
+// 1024); the four lanes scan independently.  Returns the exclusive prefix of
+// each lane and stores the four block totals in *total.
+__device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
+  __shared__ uint4 warp_sum4[32];
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint4 x = v;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-      off += v;
-      if (inc) break;
-      end -= 32;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y0 = __shfl_up_sync(0xFFFFFFFFu, x.x, o), y1 = __shfl_up_sync(0xFFFFFFFFu, x.y, o),
+                   y2 = __shfl_up_sync(0xFFFFFFFFu, x.z, o), y3 = __shfl_up_sync(0xFFFFFFFFu, x.w, o);
+    if (lane >= (uint32_t)o) { x.x += y0; x.y += y1; x.z += y2; x.w += y3; }
+  }
+  if (lane == 31) warp_sum4[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint4 w = warp_sum4[lane];  // blockDim is 1024: 32 warps
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y0 = __shfl_up_sync(0xFFFFFFFFu, w.x, o), y1 = __shfl_up_sync(0xFFFFFFFFu, w.y, o),
+                     y2 = __shfl_up_sync(0xFFFFFFFFu, w.z, o), y3 = __shfl_up_sync(0xFFFFFFFFu, w.w, o);
+      if (lane >= (uint32_t)o) { w.x += y0; w.y += y1; w.z += y2; w.w += y3; }
     }
-    if (lane == 0) {
-      if (timed_out) atomicOr(G.err, ERR_BIT_SCAN_TIMEOUT);
-      if (tile != 0) st_release_u64(&G.tstate[tile], scan_word(ep, 2u, off + tot));
-      s_off = off;
-    }
+    warp_sum4[lane] = w;  // inclusive
   }
   __syncthreads();
-  if (base < nbuckets) {
-    uint32_t run = s_off + excl;
-    uint4* rp = reinterpret_cast<uint4*>(G.range + base);  // two {start, count} pairs each
-    rp[0] = make_uint4(run, c.x, run + c.x, c.y);
-    run += c.x + c.y;
-    rp[1] = make_uint4(run, c.z, run + c.z, c.w);
+  const uint4 before = wid ? warp_sum4[wid - 1] : make_uint4(0u, 0u, 0u, 0u);
+  *total = warp_sum4[31];
+  __syncthreads();
+  return make_uint4(before.x + x.x - v.x, before.y + x.y - v.y, before.z + x.z - v.z,
+                    before.w + x.w - v.w);
+}
+
+// Persistent: each CTA takes tiles (SUBS sub-tiles of SCAN_SUB buckets,
+// SUBS = 1 or 4: small grids favour more tiles, large ones fewer) in id
+// order until none is left.  Within a tile, thread t holds buckets
+// sub * SCAN_SUB + 4t .. +3 of each sub-tile, so every load and store of a
+// warp is contiguous.
+template <uint32_t SUBS>
+__global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, uint32_t ntiles) {
+  constexpr uint32_t subs = SUBS;
+  __shared__ uint32_t s_tile, s_epoch, s_off;
+  if (threadIdx.x == 0) s_epoch = *reinterpret_cast<volatile uint32_t*>(&G.tctl[2]);
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(&G.tctl[0], 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile, ep = s_epoch & 0x3FFFFFFFu;
+    if (tile >= ntiles) break;  // uniform
+    // bucket ranges are whole multiples of 64, so each group of four counts
+    // is either all inside or all outside
+    uint4 c[4];
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+      const uint32_t base = (tile * subs + k) * SCAN_SUB + threadIdx.x * 4u;
+      c[k] = make_uint4(0u, 0u, 0u, 0u);
+      if (k < subs && base < nbuckets) {
+        uint4* cp = reinterpret_cast<uint4*>(G.count + base);
+        c[k] = *cp;
+        *cp = make_uint4(0u, 0u, 0u, 0u);  // ready for the next count pass
+      }
+    }
+    v.x = c[0].x + c[0].y + c[0].z + c[0].w;
+    v.y = c[1].x + c[1].y + c[1].z + c[1].w;
+    v.z = c[2].x + c[2].y + c[2].z + c[2].w;
+    v.w = c[3].x + c[3].y + c[3].z + c[3].w;
+    uint4 sub_tot;
+    const uint4 excl = block_exclusive_scan4(v, &sub_tot);
+    const uint32_t tot = sub_tot.x + sub_tot.y + sub_tot.z + sub_tot.w;
+    if (threadIdx.x == 0)
+      st_release_u64(&G.tstate[tile], scan_word(ep, tile == 0 ? 2u : 1u, tot));
+    if (threadIdx.x < 32u) {
+      // warp 0 looks back over windows of 32 predecessors: lane i reads tile
+      // (end - 1 - i); the window sums up to the nearest inclusive prefix
+      const uint32_t lane = threadIdx.x;
+      uint32_t off = 0;
+      int end = (int)tile;
+      const long long deadline = clock64() + WAIT_LIMIT_CYCLES;
+      bool timed_out = false;
+      while (end > 0) {
+        const int p = end - 1 - (int)lane;
+        unsigned long long w = scan_word(ep, 2u, 0u);  // before tile 0: prefix 0
+        uint32_t kind = 2u;
+        for (;;) {
+          if (p >= 0) {
+            w = ld_acquire_u64(&G.tstate[p]);
+            const uint32_t hi = (uint32_t)(w >> 32);
+            kind = (hi >> 2) == ep ? (hi & 3u) : 0u;
+          }
+          if (__all_sync(0xFFFFFFFFu, kind != 0u)) break;
+          if (__any_sync(0xFFFFFFFFu, clock64() > deadline)) {  // warp-uniform
+            timed_out = true;
+            break;
+          }
+        }
+        if (timed_out) break;
+        const uint32_t inc = __ballot_sync(0xFFFFFFFFu, kind == 2u);
+        const uint32_t stop = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest prefix
+        uint32_t s = lane <= stop ? (uint32_t)w : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+        off += s;
+        if (inc) break;
+        end -= 32;
+      }
+      if (lane == 0) {
+        if (timed_out) atomicOr(G.err, ERR_BIT_SCAN_TIMEOUT);
+        if (tile != 0) st_release_u64(&G.tstate[tile], scan_word(ep, 2u, off + tot));
+        s_off = off;
+      }
+    }
+    __syncthreads();
+    const uint32_t sub_off[4] = {0u, sub_tot.x, sub_tot.x + sub_tot.y,
+                                 sub_tot.x + sub_tot.y + sub_tot.z};
+    const uint32_t ex[4] = {excl.x, excl.y, excl.z, excl.w};
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+      const uint32_t base = (tile * subs + k) * SCAN_SUB + threadIdx.x * 4u;
+      if (k < subs && base < nbuckets) {
+        uint32_t run = s_off + sub_off[k] + ex[k];
+        uint4* rp = reinterpret_cast<uint4*>(G.range + base);  // two {start, count} pairs each
+        rp[0] = make_uint4(run, c[k].x, run + c[k].x, c[k].y);
+        run += c[k].x + c[k].y;
+        rp[1] = make_uint4(run, c[k].z, run + c[k].z, c[k].w);
+      }
+    }
+    __syncthreads();  // s_tile and s_off are rewritten by the next tile
   }
   if (threadIdx.x == 0) {
     __threadfence();
-    if (atomicAdd(&G.tctl[1], 1u) == ntiles - 1u) {  // last tile: reset for the next launch
+    if (atomicAdd(&G.tctl[1], 1u) == gridDim.x - 1u) {  // last CTA: reset for the next launch
       G.tctl[0] = 0u;
       G.tctl[1] = 0u;
       G.tctl[2] = (s_epoch + 1u) & 0x3FFFFFFFu;

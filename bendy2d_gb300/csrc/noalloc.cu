@@ -39,7 +39,7 @@ namespace {
 constexpr uint32_t NOALLOC_MAX_PARTICLES = 65536;
 constexpr uint32_t NOALLOC_MAX_BUCKETS = 2 * NOALLOC_MAX_PARTICLES;  // power of two >= 2n
 constexpr uint32_t NOALLOC_MAX_CHUNKS = NOALLOC_MAX_PARTICLES / CHUNK;
-constexpr uint32_t NOALLOC_MAX_TILES = (NOALLOC_MAX_BUCKETS + SCAN_TILE - 1) / SCAN_TILE;
+constexpr uint32_t NOALLOC_MAX_TILES = (NOALLOC_MAX_BUCKETS + SCAN_SUB - 1) / SCAN_SUB;
 
 constexpr size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 // layout of the scratch array
@@ -112,7 +112,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   uint32_t nb = 64;
   while (nb < 2 * np) nb <<= 1;
   const uint32_t nch = (np + CHUNK - 1) / CHUNK;
-  const uint32_t nt = (nb + SCAN_TILE - 1) / SCAN_TILE;
+  const uint32_t nt = (nb + SCAN_SUB - 1) / SCAN_SUB;
 
   DWorld w;
   std::memset(&w, 0, sizeof(w));
@@ -156,7 +156,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   for (uint32_t s = 0; s < w.S; ++s) {
     const uint32_t cur = s & 1u;
     k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_grid_scan<<<nt, 1024, 0, st>>>(G, nb, nt);
+    k_grid_scan<1><<<nt, 1024, 0, st>>>(G, nb, nt);  // nt <= 32 one-sub-tile tiles
     k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
     k_collide_integrate<<<nch * COLLIDE_LANES, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
   }

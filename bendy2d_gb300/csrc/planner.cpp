@@ -181,6 +181,9 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
       return bad("body link range");
     for (uint32_t i = 0; i < B.np; ++i)
       if (im.bidx[B.i0 + i] >= P.np) return bad("body particle index");
+    if (B.first != NO_FIRST &&
+        ((size_t)B.first + B.np > P.np || (B.np && im.bidx[B.i0] != B.first)))
+      return bad("body first particle");
     const uint32_t lim = B.local ? B.np : P.np;
     for (uint32_t k = 0; k < B.nl; ++k) {
       const uint2 e = im.lab[B.l0 + k];
@@ -482,6 +485,11 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
         acc += im.polys[j].nv * im.polys[i].nv;
       }
     im.stage_off.push_back(acc);
+  }
+  for (DBody& B : im.bodies) {  // contiguous particle lists load without bidx
+    B.first = B.np ? im.bidx[B.i0] : NO_FIRST;
+    for (uint32_t i = 1; i < B.np && B.first != NO_FIRST; ++i)
+      if (im.bidx[B.i0 + i] != B.first + i) B.first = NO_FIRST;
   }
   if (!check_image(im, reg, why)) return ERR_STATE;
   return OK;
