@@ -419,7 +419,16 @@ int Engine::rebuild_lists() {
   size_t np_ext = 0;
   size_t nbuckets = 0, np_pp = 0;
   uint64_t rigid_smem = 0;
-  std::map<std::tuple<uint32_t, bool, bool, uint32_t, uint32_t>, size_t> cls;
+  // Launch classes: group bodies with the same group size and kind, binned by
+  // shared bytes per group in powers of two; a class is sized to its largest
+  // member.  Few classes matter: each is a launch whose level chain costs a
+  // full link-phase latency.
+  std::map<std::tuple<uint32_t, bool, bool, bool, uint32_t>, size_t> cls;
+  auto log2c = [](uint32_t x) {
+    uint32_t b = 0;
+    while (b < 31 && (1u << b) < x) ++b;
+    return b;
+  };
   // A resident schedule takes most of an SM's shared memory (a 32x32 cloth:
   // ~170 KB, one body per SM) where a streamed one leaves room for about
   // three.  Resident schedules win when a launch has no more bodies than SMs
@@ -429,7 +438,7 @@ int Engine::rebuild_lists() {
   for (const Slot& s : slots_)
     if (s.live)
       for (const GroupBody& gb : s.img.groups)
-        if (gb.res) ++res_count[std::make_tuple(gb.T, !s.img.ext, class_region(gb.region))];
+        if (gb.res) ++res_count[std::make_tuple(gb.T, !s.img.ext, log2c(gb.region + gb.res))];
   wlaunch_.assign(slots_.size(), WorldLaunch());
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
@@ -441,34 +450,27 @@ int Engine::rebuild_lists() {
     wlaunch_[si].sf0 = (uint32_t)serial_full_.size();
     wlaunch_[si].pk0 = (uint32_t)packs_full_.packs.size();
     for (const GroupBody& gb : im.groups) {
-      const uint32_t rc = gb.smem ? class_region(gb.region) : 0u;
       const bool use_res =
-          gb.res && res_count[std::make_tuple(gb.T, full, rc)] <= (size_t)std::max(g_num_sms, 1);
-      const uint32_t rs = use_res ? class_res(gb.res) : 0u;
-      auto key = std::make_tuple(gb.T, gb.smem, full, rc, rs);
+          gb.res && res_count[std::make_tuple(gb.T, full, log2c(gb.region + gb.res))] <=
+                        (size_t)std::max(g_num_sms, 1);
+      const uint32_t bin = gb.smem ? log2c(gb.region + (use_res ? gb.res : 0u)) : 0u;
+      auto key = std::make_tuple(gb.T, gb.smem, full, use_res, bin);
       auto it = cls.find(key);
       if (it == cls.end()) {
         LaunchClass c;
         c.T = gb.T;
         c.smem = gb.smem;
         c.full = full;
-        c.res = rs;
-        if (rs) {
-          c.region = rc;  // the planner checked rc + rs + tail against the limit
-        } else {
-          c.region = gb.smem ? std::min<uint32_t>(rc, tune_.smem_max) : 0u;
-          if (gb.smem && c.region < gb.region) c.region = gb.region;
-        }
-        const uint32_t per_group = c.region + (rs ? rs : STREAM_BUF_BYTES) + GROUP_TAIL_BYTES;
-        uint32_t G = gb.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / gb.T);
-        if (gb.T != 32) G = std::min<uint32_t>(G, std::min<uint32_t>(tune_.max_groups, 15));
-        G = std::max<uint32_t>(G, 1);
-        G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / per_group));
-        c.G = G;
+        c.region = 0;
+        c.res = 0;
+        c.G = 1;
         it = cls.emplace(key, classes_.size()).first;
         classes_.push_back(std::move(c));
       }
-      classes_[it->second].items.push_back(make_uint2(si, gb.body));
+      LaunchClass& c = classes_[it->second];
+      if (gb.smem) c.region = std::max(c.region, gb.region);
+      if (use_res) c.res = std::max(c.res, gb.res);
+      c.items.push_back(make_uint2(si, gb.body));
     }
     if (plain_ && full) {  // plain mode: this world's own packs
       std::vector<uint2> mine;
@@ -521,6 +523,16 @@ int Engine::rebuild_lists() {
       for (uint32_t st = 0; st < im.params.np; st += CHUNK) chunks_.push_back(make_uint2(si, st));
       np_ext += im.params.np;
     }
+  }
+  // size each class to its largest member; a resident class whose largest
+  // body and largest schedule do not fit together streams instead
+  for (LaunchClass& c : classes_) {
+    if (c.res && (size_t)c.region + c.res + GROUP_TAIL_BYTES > (size_t)g_smem_optin) c.res = 0;
+    const uint32_t per_group = c.region + (c.res ? c.res : STREAM_BUF_BYTES) + GROUP_TAIL_BYTES;
+    uint32_t G = c.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / c.T);
+    if (c.T != 32) G = std::min<uint32_t>(G, std::min<uint32_t>(tune_.max_groups, 15));
+    G = std::max<uint32_t>(G, 1);
+    c.G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / per_group));
   }
   if (!plain_) build_packs(sfull_all, true, packs_full_, serial_full_);
   build_packs(slinks_all, false, packs_links_, serial_links_);
@@ -632,9 +644,13 @@ int Engine::launch_all(bool profiling) {
   // before the pass, and all joined back before the grid and collide kernels.
   uint32_t br_used = 0, br_next = 0;
   cudaEvent_t fork_ev = nullptr;
-  auto begin_pass = [&]() {
+  auto begin_pass = [&](bool full) {
     br_used = br_next = 0;
     if (profiling) return;
+    size_t n = full ? (packs_full_.packs.empty() ? 0 : 1) + (serial_full_.empty() ? 0 : 1)
+                    : (packs_links_.packs.empty() ? 0 : 1) + (serial_links_.empty() ? 0 : 1);
+    for (const LaunchClass& c : classes_) n += (c.full == full && !c.items.empty()) ? 1 : 0;
+    if (n < 2) return;  // a single launch stays on the main stream
     fork_ev = evpool_[evi++ % evpool_.size()];
     cudaEventRecord(fork_ev, stream_);
   };
@@ -712,7 +728,7 @@ int Engine::launch_all(bool profiling) {
     }
   } else {
   // worlds without extension collisions: one launch per class for the whole step
-  begin_pass();
+  begin_pass(true);
   groups(true, 0, 0);
   if (!packs_full_.packs.empty()) {
     const SerialPacks& P = packs_full_;
@@ -749,7 +765,7 @@ int Engine::launch_all(bool profiling) {
         else k_rigid<3><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
       });
     }
-    begin_pass();
+    begin_pass(false);
     groups(false, cur, s);
     if (!packs_links_.packs.empty()) {
       const SerialPacks& P = packs_links_;

@@ -50,11 +50,6 @@ struct GroupBody {
   bool smem;
 };
 
-// Launch classes round their members' shared-memory needs up to these steps
-// (body region, resident schedule); the planner applies the same rounding
-// when it decides whether a schedule fits.
-inline uint32_t class_region(uint32_t r) { return (r + 4095u) & ~4095u; }
-inline uint32_t class_res(uint32_t r) { return (r + 8191u) & ~8191u; }
 
 struct PlanStats {
   uint32_t bodies = 0, group_bodies = 0, serial_bodies = 0, global_bodies = 0;
@@ -164,7 +159,7 @@ class Engine {
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
   cudaStream_t aux_[2] = {nullptr, nullptr};  // graph branches (circles/polygons)
-  static constexpr uint32_t kLinkBranches = 3;
+  static constexpr uint32_t kLinkBranches = 7;
   cudaStream_t lx_[kLinkBranches] = {};       // graph branches of the link phase
   std::vector<struct CUevent_st*> evpool_;
   PlanTuning tune_;

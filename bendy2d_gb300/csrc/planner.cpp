@@ -362,8 +362,7 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
     uint32_t res = 0;
     if (smem && tune.resident) {
       const size_t sb = (size_t)S.words * 4u;
-      if ((size_t)class_region((uint32_t)region) + class_res((uint32_t)sb) + GROUP_TAIL_BYTES <=
-          tune.res_max)
+      if (region + sb + GROUP_TAIL_BYTES <= tune.res_max)
         res = (uint32_t)sb;
     }
     B.local = smem ? 1u : 0u;
