@@ -396,6 +396,13 @@ def main():
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get(dom)
+    # the link executor is bound by its level chain, not by memory: levels per
+    # launch (one body) and the time each level takes
+    chain = None
+    if dom.startswith("exec_groups"):
+        st = s.plan_stats()
+        lv = st["levels"] / max(1, st["group_bodies"])
+        chain = {"levels_per_launch": lv, "ns_per_level": dom_ms * 1e6 / lv}
 
     if rank != 0:
         if world > 1:
@@ -440,7 +447,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": alg,
-                     "launch_ms": dom_ms},
+                     "launch_ms": dom_ms, "chain": chain},
         "kernel_ms_per_step": {k: v / nprof for k, v in sorted(prof_tot.items())},
         "gpu_launches": launches,
         "clocks": clk.summary(),
