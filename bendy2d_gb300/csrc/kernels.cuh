@@ -1406,6 +1406,7 @@ static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
   const bool own = act && lane == 0;  // the lane that owns particle i
   const float2* P = W.pos[cur];
   float2 p = act ? P[i] : make_float2(0.f, 0.f);
+  float2 q = own ? W.prev[i] : make_float2(0.f, 0.f);  // issued early, used last
   if (W.flags & COLLIDE_PP) {  // uniform over the CTA
     long long sx = 0, sy = 0;
     bool hit = false;
@@ -1457,7 +1458,6 @@ static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
     }
   }
   if (!own) return;
-  float2 q = W.prev[i];
   solve_bounds(p, q, W);
   integrate(p, q, W.gx, W.gy, W.h);
   W.pos[cur ^ 1u][i] = p;
