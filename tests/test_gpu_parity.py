@@ -252,6 +252,29 @@ def test_batch_equals_alone(gpu):
     b.close()
 
 
+def test_mixed_batch_matches_oracle(gpu):
+    """A batch mixing one world of 160 cloth bodies (more than there are SMs:
+    its launch class streams schedules) with serving-style worlds of mixed
+    sizes (small classes hold schedules resident and run on branch streams),
+    all with particle collisions: every world matches the oracle."""
+    from bendy2d_gb300 import Batch, scenes
+    from oracle import load_scene
+    rng = np.random.default_rng(41)
+    worlds = [scenes.config2(seed=9, n_bodies=160, collide=1)]
+    worlds += [scenes.config4_request(rng, int(n))
+               for n in np.exp(rng.uniform(np.log(64), np.log(6000), 20)).astype(int)]
+    sols = [w.to_solver() for w in worlds]
+    b = Batch(sols)
+    for _ in range(2):
+        b.update(worlds[0].dt)
+    for w, s in zip(worlds, sols):
+        o = load_scene(w)
+        for _ in range(2):
+            assert o.update(w.dt) == 0
+        assert_same_state(solver_state(s), oracle_state(o), f"mixed batch {w.name}")
+    b.close()
+
+
 def test_plain_mode_equals_batched(gpu):
     """The one-world-per-launch baseline computes the same bits."""
     from bendy2d_gb300 import Batch, scenes
