@@ -463,6 +463,8 @@ int Engine::rebuild_lists() {
         c.full = full;
         c.region = 0;
         c.res = 0;
+        c.fill = 0;
+        c.words = 0;
         c.G = 1;
         it = cls.emplace(key, classes_.size()).first;
         classes_.push_back(std::move(c));
@@ -470,6 +472,7 @@ int Engine::rebuild_lists() {
       LaunchClass& c = classes_[it->second];
       if (gb.smem) c.region = std::max(c.region, gb.region);
       if (use_res) c.res = std::max(c.res, gb.res);
+      c.words = std::max(c.words, reg_.scheds[im.bodies[gb.body].sched].words);
       c.items.push_back(make_uint2(si, gb.body));
     }
     if (plain_ && full) {  // plain mode: this world's own packs
@@ -528,7 +531,16 @@ int Engine::rebuild_lists() {
   // body and largest schedule do not fit together streams instead
   for (LaunchClass& c : classes_) {
     if (c.res && (size_t)c.region + c.res + GROUP_TAIL_BYTES > (size_t)g_smem_optin) c.res = 0;
-    const uint32_t per_group = c.region + (c.res ? c.res : STREAM_BUF_BYTES) + GROUP_TAIL_BYTES;
+    // streamed: one 16 KB chunk per fill, or for launches with no more bodies
+    // than SMs (latency-bound) the largest fills that fit beside the body,
+    // which cuts the buffer switches of long schedules
+    c.fill = STREAM_BUF_BYTES / 2;
+    if (!c.res && c.items.size() <= (size_t)std::max(g_num_sms, 1)) {
+      const uint32_t room = ((uint32_t)g_smem_optin - c.region - GROUP_TAIL_BYTES) / 2 & ~15u;
+      const uint32_t want = (c.words * 4u + 15u) & ~15u;
+      c.fill = std::max(c.fill, std::min(room, want));
+    }
+    const uint32_t per_group = c.region + (c.res ? c.res : 2 * c.fill) + GROUP_TAIL_BYTES;
     uint32_t G = c.T == 32 ? tune_.warp_groups : std::max<uint32_t>(1, 256 / c.T);
     if (c.T != 32) G = std::min<uint32_t>(G, std::min<uint32_t>(tune_.max_groups, 15));
     G = std::max<uint32_t>(G, 1);
@@ -673,7 +685,7 @@ int Engine::launch_all(bool profiling) {
   auto launch_class = [&](const LaunchClass& c, const uint2* L, uint32_t n, uint32_t cur,
                           uint32_t sub, cudaStream_t st) {
     const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
-    const uint32_t sb = c.res ? c.res : STREAM_BUF_BYTES;
+    const uint32_t sb = c.res ? c.res : 2 * c.fill;
     const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
     const uint32_t rg = c.smem ? c.region : 0u;
     if (c.res && c.full) k_exec_groups<true, true, true><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);

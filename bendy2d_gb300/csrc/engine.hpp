@@ -98,7 +98,9 @@ void write_block(const WorldImage& im, const BlockLayout& L, unsigned char* dst)
 
 struct LaunchClass {
   uint32_t T, G, region;
-  uint32_t res;  // resident schedule bytes per group (0: streamed in chunks)
+  uint32_t res;    // resident schedule bytes per group (0: streamed in fills)
+  uint32_t fill;   // streamed: bytes per fill buffer (two per group)
+  uint32_t words;  // largest member schedule, in words
   bool smem, full;
   std::vector<uint2> items;
   size_t dev_off = 0;  // offset (in uint2) into the device list buffer

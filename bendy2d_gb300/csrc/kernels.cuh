@@ -150,10 +150,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return true;
 }
 
-// shared bytes per group beyond the body region when the schedule streams:
-// two chunk buffers, then two mbarriers and two flag words (GROUP_TAIL_BYTES)
+// shared bytes per group beyond the body region when the schedule streams
+// in fills of one chunk: two chunk buffers, then GROUP_TAIL_BYTES (two
+// mbarriers, a flag word and the chunk count of each buffer)
 constexpr uint32_t STREAM_BUF_BYTES = 2 * SCHED_CHUNK_WORDS * 4;
-constexpr uint32_t STREAM_BYTES = STREAM_BUF_BYTES + 32;
+constexpr uint32_t STREAM_BYTES = STREAM_BUF_BYTES + GROUP_TAIL_BYTES;
 
 // ----------------------------------------------------------------------------
 // Body executor (block / warp granularity).
@@ -218,16 +219,39 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
 
   // per group: body region | schedule area (sched_bytes: the whole schedule
-  // when RES, else two chunk buffers) | two mbarriers and two flag words
+  // when RES, else two fill buffers) | two mbarriers, a flag word and the
+  // chunk count of each fill buffer
   unsigned char* base = smem + (size_t)g * (region_bytes + sched_bytes + GROUP_TAIL_BYTES);
   uint32_t* cbuf = reinterpret_cast<uint32_t*>(base + region_bytes);
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + region_bytes + sched_bytes);
   volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(bar + 2);
+  volatile uint32_t* fill_n = flag + 2;
+  // Streamed schedules arrive in fills: as many whole consecutive chunks as
+  // one buffer of fill_words holds (a schedule's chunks are contiguous, so a
+  // fill is one bulk copy).  Thread 0 issues fill c.. into buffer k2 and
+  // returns the first chunk of the next fill.
+  const uint32_t fill_words = sched_bytes / 8u;
+  auto issue_fill = [&](uint32_t c, uint32_t k2) {
+    uint32_t w = 0, e = c;
+    while (e < S.nchunks) {
+      const uint32_t l = SC.chunk_len[S.chunk0 + e];
+      if (e > c && w + l > fill_words) break;
+      w += l;
+      ++e;
+    }
+    fill_n[k2] = e - c;
+    bulk_load(cbuf + k2 * fill_words, SC.stream + SC.chunk_off[S.chunk0 + c], w * 4u, &bar[k2]);
+    return e;
+  };
+  uint32_t next_c = 0;  // thread 0: first chunk not yet issued
   if (t == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
-    if (S.nchunks > 0) bulk_load(cbuf, SC.stream + S.off, (RES ? S.words : S.len0) * 4u, &bar[0]);
+    if (S.nchunks > 0) {
+      if (RES) bulk_load(cbuf, SC.stream + S.off, S.words * 4u, &bar[0]);
+      else next_c = issue_fill(0u, 0u);
+    }
   }
   // body state in shared memory: pos[np], prev[np] (FULL), {rest, stiff}[nl]
   const uint32_t sp_a = smem_addr(base);
@@ -331,11 +355,12 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     uint32_t buf_a = cbuf_a;
     for (uint32_t c = 0; c < S.nchunks; ++c) buf_a = run_chunk(buf_a);
   } else {
-    // buffer k2 = c & 1 is used for the (c >> 1)-th time: its mbarrier
-    // phase parity is (c >> 1) & 1
-    for (uint32_t c = 0; c < S.nchunks; ++c) {
-      const uint32_t k2 = c & 1u;
-      const uint32_t par = (c >> 1) & 1u;
+    // buffer k2 = f & 1 holds fill f, used for the (f >> 1)-th time: its
+    // mbarrier phase parity is (f >> 1) & 1
+    uint32_t c = 0;
+    for (uint32_t f = 0; c < S.nchunks; ++f) {
+      const uint32_t k2 = f & 1u;
+      const uint32_t par = (f >> 1) & 1u;
       if (t == 0) flag[0] = mbar_wait_bounded(&bar[k2], par) ? 1u : 0u;
       group_sync(g, T);
       if (flag[0] == 0u) {
@@ -346,12 +371,14 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
         return;  // every thread of the group leaves together
       }
       mbar_try(&bar[k2], par);  // completed phase: makes the data visible here
-      if (t == 0 && c + 1 < S.nchunks) {
+      const uint32_t n = fill_n[k2];
+      if (t == 0 && next_c < S.nchunks) {  // the other buffer is free: next fill
         fence_proxy_async();
-        bulk_load(cbuf + (k2 ^ 1u) * SCHED_CHUNK_WORDS, SC.stream + SC.chunk_off[S.chunk0 + c + 1],
-                  SC.chunk_len[S.chunk0 + c + 1] * 4u, &bar[k2 ^ 1u]);
+        next_c = issue_fill(next_c, k2 ^ 1u);
       }
-      run_chunk(cbuf_a + k2 * SCHED_CHUNK_WORDS * 4u);
+      uint32_t buf_a = cbuf_a + k2 * fill_words * 4u;
+      for (uint32_t j = 0; j < n; ++j) buf_a = run_chunk(buf_a);
+      c += n;
     }
   }
 
