@@ -123,6 +123,25 @@ def algorithmic_bytes(kernel: str, sc) -> float:
     return 0.0
 
 
+def step_bytes_per_unit(sc) -> float:
+    """Algorithmic HBM bytes of a whole update per particle-substep:
+    bounds+integrate 32 B, plus per link and iteration 12 B (endpoints, rest)
+    or 16 B (with a stiffness other than 1) and 32 B (read+write of both
+    positions)."""
+    n, l = sc.n_particles, len(sc.la)
+    s = 16.0 if np.any(np.asarray(sc.stiff) != 1.0) else 12.0
+    return 32.0 + sc.link_iters * (l / max(n, 1)) * (s + 32.0)
+
+
+def step_roofline(value: float, bytes_per_unit: float) -> dict:
+    """Whole-update roofline: algorithmic bytes x particle-substeps/s
+    against the measured HBM copy bandwidth."""
+    peak, kind = _peaks()
+    gbs = value * bytes_per_unit / 1e9
+    return {"bound": "hbm", "bytes_per_unit": bytes_per_unit, "achieved": gbs, "peak": peak,
+            "unit": "GB/s", "frac": gbs / peak, "peak_source": kind}
+
+
 def run_cpu_oracle(sc, budget_s: float, max_steps: int = 1000):
     from oracle import load_scene
     o = load_scene(sc)
@@ -150,7 +169,7 @@ def run_batched_comparison(args, torch, flush, stream):
     dt = worlds[0].dt
     out = {"workload": f"{len(worlds)} worlds of 1-8 hub-and-spoke rings, particles "
                        "log-uniform in [64, 4096], 2 circles + floor polygon each, 8 sub-steps, "
-                       "1 link iteration", "worlds": len(worlds),
+                       "1 link iteration (batched_i4: 4)", "worlds": len(worlds),
            "particles": int(sum(w.n_particles for w in worlds))}
 
     def timed_steps(batch, k):
@@ -172,9 +191,24 @@ def run_batched_comparison(args, torch, flush, stream):
     for _ in range(3):
         b.update(dt)
     ms = timed_steps(b, args.batched_steps)
+    bpu = sum(step_bytes_per_unit(w) * w.n_particles for w in worlds) / \
+        max(1, sum(w.n_particles for w in worlds))
     out["batched"] = {"value": units / (ms / 1e3), "ms_per_step": ms,
-                      "launches_per_step": b.launch_count()}
+                      "launches_per_step": b.launch_count(),
+                      "roofline": step_roofline(units / (ms / 1e3), bpu)}
     b.close()
+    # the same worlds with 4 link iterations (batched only)
+    w4 = scenes.config3(seed=0, n_worlds=args.batched_worlds, link_iters=4)
+    b4 = Batch([w.to_solver() for w in w4])
+    b4.set_stream(stream.cuda_stream)
+    for _ in range(3):
+        b4.update(dt)
+    ms4 = timed_steps(b4, args.batched_steps)
+    bpu4 = sum(step_bytes_per_unit(w) * w.n_particles for w in w4) / \
+        max(1, sum(w.n_particles for w in w4))
+    out["batched_i4"] = {"value": units / (ms4 / 1e3), "ms_per_step": ms4,
+                         "roofline": step_roofline(units / (ms4 / 1e3), bpu4)}
+    b4.close()
     p = Batch([w.to_solver() for w in worlds])
     p.set_plain(True)
     p.set_stream(stream.cuda_stream)
@@ -236,9 +270,11 @@ def run_config5(args, torch, flush, stream):
         s.synchronize()
         torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-        out[name] = {"value": sc.n_particles * sc.sub_steps / (ms / 1e3), "ms_per_step": ms,
+        v = sc.n_particles * sc.sub_steps / (ms / 1e3)
+        out[name] = {"value": v, "ms_per_step": ms,
                      "residual_after": link_residual(s, sc),
-                     "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024}
+                     "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024,
+                     "roofline": step_roofline(v, step_bytes_per_unit(sc))}
         s.close()
     return out
 
