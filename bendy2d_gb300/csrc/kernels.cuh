@@ -401,6 +401,57 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 // whole group would idle.  This variant works on global memory (bodies too
 // large for a shared-memory pack).
 // ----------------------------------------------------------------------------
+// One body's link passes replayed in insertion order by one thread,
+// software-pipelined: the next link's endpoints and parameters are loaded
+// before the current solve, and an endpoint the current link writes is taken
+// from registers instead of memory.  So each step of a chain (consecutive
+// links sharing a particle: ring rims, spokes into a hub) costs the solve
+// alone, not solve + store + reload; values are the same as the plain loop's.
+// P maps a body-local particle index to its storage (shared or global).
+template <typename P>
+__device__ __forceinline__ void serial_link_passes(P pos, const uint2* __restrict__ ab,
+                                                   const float* __restrict__ rest,
+                                                   const float* __restrict__ stiff, uint32_t nl,
+                                                   uint32_t I) {
+  if (nl == 0) return;
+  for (uint32_t it = 0; it < I; ++it) {
+    uint2 e = __ldg(ab);
+    float r = __ldg(rest), st = __ldg(stiff);
+    float2 pa = pos.get(e.x), pb = pos.get(e.y);
+    for (uint32_t k = 0; k < nl; ++k) {
+      const bool more = k + 1 < nl;
+      const uint2 en = more ? __ldg(ab + k + 1) : e;
+      const float rn = more ? __ldg(rest + k + 1) : r;
+      const float sn = more ? __ldg(stiff + k + 1) : st;
+      // the next link's endpoints that this link does not write
+      const bool fa = en.x == e.x || en.x == e.y, fb = en.y == e.x || en.y == e.y;
+      float2 qa = fa ? make_float2(0.f, 0.f) : pos.get(en.x);
+      float2 qb = fb ? make_float2(0.f, 0.f) : pos.get(en.y);
+      link_solve(pa, pb, r, st);
+      pos.put(e.x, pa);
+      pos.put(e.y, pb);
+      if (fa) qa = en.x == e.x ? pa : pb;
+      if (fb) qb = en.y == e.x ? pa : pb;
+      e = en;
+      r = rn;
+      st = sn;
+      pa = qa;
+      pb = qb;
+    }
+  }
+}
+struct SmemPos {
+  float2* p;
+  __device__ float2 get(uint32_t i) const { return p[i]; }
+  __device__ void put(uint32_t i, float2 v) const { p[i] = v; }
+};
+struct GlobalPos {
+  float2* p;
+  const uint32_t* bidx;
+  __device__ float2 get(uint32_t i) const { return p[bidx[i]]; }
+  __device__ void put(uint32_t i, float2 v) const { p[bidx[i]] = v; }
+};
+
 template <bool FULL>
 __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __restrict__ list,
                               uint32_t n, uint32_t cur, uint32_t sub) {
@@ -421,16 +472,7 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
   DWorld Wb;
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
   for (uint32_t s = 0; s < nsub; ++s) {
-    for (uint32_t it = 0; it < I; ++it) {
-      for (uint32_t k = 0; k < B.nl; ++k) {
-        const uint2 e = ab[k];  // body-local endpoints
-        const uint32_t ia = bidx[e.x], ib = bidx[e.y];
-        float2 pa = p[ia], pb = p[ib];
-        link_solve(pa, pb, rest[k], stiff[k]);
-        p[ia] = pa;
-        p[ib] = pb;
-      }
-    }
+    serial_link_passes(GlobalPos{p, bidx}, ab, rest, stiff, B.nl, I);  // body-local endpoints
     if (FULL) {
       for (uint32_t k = 0; k < B.np; ++k) {
         const uint32_t j = bidx[k];
@@ -496,15 +538,7 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
       DWorld Wb;
       Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
       for (uint32_t s = 0; s < nsub; ++s) {
-        for (uint32_t it = 0; it < I; ++it) {
-          for (uint32_t k = 0; k < B.nl; ++k) {
-            const uint2 e = __ldg(ab + k);
-            float2 pa = p[e.x], pb = p[e.y];
-            link_solve(pa, pb, __ldg(rest + k), __ldg(stiff + k));
-            p[e.x] = pa;
-            p[e.y] = pb;
-          }
-        }
+        serial_link_passes(SmemPos{p}, ab, rest, stiff, B.nl, I);
         if (FULL) {
           for (uint32_t k = 0; k < B.np; ++k) {
             float2 pp = p[k], qq = q[k];
