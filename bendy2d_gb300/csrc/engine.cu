@@ -40,7 +40,7 @@ static uint32_t pow2ceil_u(uint32_t x) {
 static int g_smem_optin = -1;
 static int g_num_sms = 0;
 static constexpr uint64_t kRigidSmemCap = 96 * 1024;
-static constexpr uint32_t kSerialPackBytes = 96 * 1024;  // shared memory per serial pack
+static constexpr uint32_t kSerialPackBytes = 96 * 1024;  // shared memory per small-body pack
 static constexpr uint32_t kSerialPackThreads = 64;       // bodies per serial pack
 
 Engine::Engine(cudaStream_t stream) : stream_(stream) {
@@ -60,8 +60,9 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     for (auto fn : {k_rigid<0>, k_rigid<1>, k_rigid<2>, k_rigid<3>})
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRigidSmemCap);
-    for (auto fn : {k_exec_serial_smem<true>, k_exec_serial_smem<false>})
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSerialPackBytes);
+    for (auto fn : {k_exec_serial_smem<true, false>, k_exec_serial_smem<false, false>,
+                    k_exec_serial_smem<true, true>, k_exec_serial_smem<false, true>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
     for (auto fn : {k_exec_groups<true, true, false>, k_exec_groups<false, true, false>,
                     k_exec_groups<true, false, false>, k_exec_groups<false, false, false>,
                     k_exec_groups<true, true, true>, k_exec_groups<false, true, true>})
@@ -365,17 +366,51 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
 // First-fit decreasing: bodies sorted by size, each into the first pack with
 // room (bytes and threads).  Bodies larger than a pack stay in `rest` for the
 // global-memory serial kernel.
-void Engine::build_packs(std::vector<uint2>& in, bool full, SerialPacks& out,
-                         std::vector<uint2>& rest) {
+// Serial packs.  The step time of a batch of chain-like bodies follows its
+// longest chains.  A body whose chain is at least stage_frac (default 2/3)
+// of the longest gets a pack of its own with the links staged too (8 or 16 B
+// per particle plus 16 B per link, up to the shared-memory limit; at most
+// one per SM; allow_large): staging cuts a link from ~333 to ~211 cycles, so
+// shorter chains finish in time without it and leave the SMs' shared memory
+// to the packs of many bodies (positions only, first-fit decreasing, up to
+// kSerialPackBytes and kSerialPackThreads bodies).  What fits neither stays
+// in `rest` for the global-memory serial kernel.
+void Engine::build_packs(std::vector<uint2>& in, bool full, SerialPacks* out,
+                         std::vector<uint2>& rest, bool allow_large) {
   const uint32_t per = full ? 16u : 8u;
-  auto np_of = [&](const uint2& it) { return slots_[it.x].img.bodies[it.y].np; };
+  auto body = [&](const uint2& it) -> const DBody& { return slots_[it.x].img.bodies[it.y]; };
+  auto bytes_of = [&](const uint2& it) { return body(it).np * per + body(it).nl * 16u; };
   std::stable_sort(in.begin(), in.end(),
-                   [&](const uint2& a, const uint2& b) { return np_of(a) > np_of(b); });
+                   [&](const uint2& a, const uint2& b) { return bytes_of(a) > bytes_of(b); });
+  const uint32_t large_cap = allow_large ? (uint32_t)g_smem_optin : 0u;
+  size_t n_large = 0;
+  const size_t max_large = (size_t)std::max(g_num_sms, 1);
+  uint64_t max_links = 0;
+  for (const uint2& it : in) max_links = std::max<uint64_t>(max_links, (uint64_t)body(it).nl);
+  auto long_chain = [&](const uint2& it) {
+    return (double)body(it).nl >= (double)tune_.stage_frac * (double)max_links;
+  };
   std::vector<std::vector<uint2>> bins;
   std::vector<uint32_t> used;
   size_t first_open = 0;
+  auto emit = [&](SerialPacks& o, const std::vector<uint2>& bin, bool staged) {
+    o.packs.push_back(make_uint2((uint32_t)o.items.size(), (uint32_t)bin.size()));
+    uint32_t pb = 0, lb = 0;
+    for (const uint2& it : bin) {
+      o.items.push_back(it);
+      o.base.push_back(make_uint2(pb, lb));
+      pb += body(it).np;
+      lb += body(it).nl;
+    }
+    o.max_bytes = std::max(o.max_bytes, pb * per + (staged ? lb * 16u : 0u));
+  };
   for (const uint2& it : in) {
-    const uint32_t bytes = np_of(it) * per;
+    if (n_large < max_large && long_chain(it) && bytes_of(it) <= large_cap) {  // longest chains
+      emit(out[1], std::vector<uint2>{it}, true);
+      ++n_large;
+      continue;
+    }
+    const uint32_t bytes = body(it).np * per;
     if (bytes > kSerialPackBytes) {
       rest.push_back(it);
       continue;
@@ -392,24 +427,14 @@ void Engine::build_packs(std::vector<uint2>& in, bool full, SerialPacks& out,
     used[k] += bytes;
     while (first_open < bins.size() && bins[first_open].size() >= kSerialPackThreads) ++first_open;
   }
-  for (size_t k = 0; k < bins.size(); ++k) {
-    out.packs.push_back(make_uint2((uint32_t)out.items.size(), (uint32_t)bins[k].size()));
-    uint32_t base = 0;
-    for (const uint2& it : bins[k]) {
-      out.items.push_back(it);
-      out.sbase.push_back(base);
-      base += np_of(it);
-    }
-    out.max_bytes = std::max(out.max_bytes, base * per);
-  }
+  for (const auto& bin : bins) emit(out[0], bin, false);
 }
 
 int Engine::rebuild_lists() {
   classes_.clear();
   serial_full_.clear();
   serial_links_.clear();
-  packs_full_ = SerialPacks();
-  packs_links_ = SerialPacks();
+  for (int k = 0; k < 2; ++k) packs_full_[k] = packs_links_[k] = SerialPacks();
   std::vector<uint2> sfull_all, slinks_all;
   chunks_.clear();
   rigid_full_.clear();
@@ -448,7 +473,7 @@ int Engine::rebuild_lists() {
     std::vector<size_t> cls_before(classes_.size());
     for (size_t c = 0; c < classes_.size(); ++c) cls_before[c] = classes_[c].items.size();
     wlaunch_[si].sf0 = (uint32_t)serial_full_.size();
-    wlaunch_[si].pk0 = (uint32_t)packs_full_.packs.size();
+    wlaunch_[si].pk0 = (uint32_t)packs_full_[0].packs.size();
     for (const GroupBody& gb : im.groups) {
       const bool use_res =
           gb.res && res_count[std::make_tuple(gb.T, full, log2c(gb.region + gb.res))] <=
@@ -478,12 +503,12 @@ int Engine::rebuild_lists() {
     if (plain_ && full) {  // plain mode: this world's own packs
       std::vector<uint2> mine;
       for (uint32_t b : im.serials) mine.push_back(make_uint2(si, b));
-      build_packs(mine, true, packs_full_, serial_full_);
+      build_packs(mine, true, packs_full_, serial_full_, false);  // small packs only
     } else {
       for (uint32_t b : im.serials) (full ? sfull_all : slinks_all).push_back(make_uint2(si, b));
     }
     wlaunch_[si].sfn = (uint32_t)serial_full_.size() - wlaunch_[si].sf0;
-    wlaunch_[si].pkn = (uint32_t)packs_full_.packs.size() - wlaunch_[si].pk0;
+    wlaunch_[si].pkn = (uint32_t)packs_full_[0].packs.size() - wlaunch_[si].pk0;
     for (size_t c = 0; c < classes_.size(); ++c) {
       const size_t before = c < cls_before.size() ? cls_before[c] : 0;
       if (classes_[c].items.size() > before)
@@ -546,8 +571,8 @@ int Engine::rebuild_lists() {
     G = std::max<uint32_t>(G, 1);
     c.G = std::max<uint32_t>(1, std::min<uint32_t>(G, (uint32_t)g_smem_optin / per_group));
   }
-  if (!plain_) build_packs(sfull_all, true, packs_full_, serial_full_);
-  build_packs(slinks_all, false, packs_links_, serial_links_);
+  if (!plain_) build_packs(sfull_all, true, packs_full_, serial_full_, true);
+  build_packs(slinks_all, false, packs_links_, serial_links_, true);
   // sort serial items longest first (load balance)
   auto serial_cost = [&](const uint2& a) {
     const DBody& B = slots_[a.x].img.bodies[a.y];
@@ -570,19 +595,17 @@ int Engine::rebuild_lists() {
   all.insert(all.end(), serial_links_.begin(), serial_links_.end());
   off_chunks_ = all.size();
   all.insert(all.end(), chunks_.begin(), chunks_.end());
-  for (SerialPacks* sp : {&packs_full_, &packs_links_}) {
+  for (SerialPacks* sp : {&packs_full_[0], &packs_full_[1], &packs_links_[0], &packs_links_[1]}) {
     sp->off_items = all.size();
     all.insert(all.end(), sp->items.begin(), sp->items.end());
     sp->off_packs = all.size();
     all.insert(all.end(), sp->packs.begin(), sp->packs.end());
+    sp->off_base = all.size();
+    all.insert(all.end(), sp->base.begin(), sp->base.end());
   }
   std::vector<uint32_t> wl(rigid_full_);
   off_rigid_ext_ = wl.size();
   wl.insert(wl.end(), rigid_ext_.begin(), rigid_ext_.end());
-  for (SerialPacks* sp : {&packs_full_, &packs_links_}) {
-    sp->off_sbase = wl.size();
-    wl.insert(wl.end(), sp->sbase.begin(), sp->sbase.end());
-  }
   if (all.size() > lists_cap_) {
     B2D_CUDA(cudaStreamSynchronize(stream_));
     cudaFree(d_lists_);
@@ -659,8 +682,9 @@ int Engine::launch_all(bool profiling) {
   auto begin_pass = [&](bool full) {
     br_used = br_next = 0;
     if (profiling) return;
-    size_t n = full ? (packs_full_.packs.empty() ? 0 : 1) + (serial_full_.empty() ? 0 : 1)
-                    : (packs_links_.packs.empty() ? 0 : 1) + (serial_links_.empty() ? 0 : 1);
+    const SerialPacks* pk = full ? packs_full_ : packs_links_;
+    size_t n = (pk[0].packs.empty() ? 0 : 1) + (pk[1].packs.empty() ? 0 : 1) +
+               ((full ? serial_full_ : serial_links_).empty() ? 0 : 1);
     for (const LaunchClass& c : classes_) n += (c.full == full && !c.items.empty()) ? 1 : 0;
     if (n < 2) return;  // a single launch stays on the main stream
     fork_ev = evpool_[evi++ % evpool_.size()];
@@ -719,10 +743,10 @@ int Engine::launch_all(bool profiling) {
         timed("plain_exec_groups", [&] { launch_class(lc, L, n, 0, 0, stream_); });
       }
       if (wl.pkn) {
-        const SerialPacks& P = packs_full_;
+        const SerialPacks& P = packs_full_[0];
         timed("plain_exec_serial_smem", [&] {
-          k_exec_serial_smem<true><<<wl.pkn, kSerialPackThreads, P.max_bytes, stream_>>>(
-              W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs + wl.pk0,
+          k_exec_serial_smem<true, false><<<wl.pkn, kSerialPackThreads, P.max_bytes, stream_>>>(
+              W, d_lists_ + P.off_items, d_lists_ + P.off_base, d_lists_ + P.off_packs + wl.pk0,
               wl.pkn, 0, 0);
         });
       }
@@ -742,13 +766,16 @@ int Engine::launch_all(bool profiling) {
   // worlds without extension collisions: one launch per class for the whole step
   begin_pass(true);
   groups(true, 0, 0);
-  if (!packs_full_.packs.empty()) {
-    const SerialPacks& P = packs_full_;
+  for (int k = 0; k < 2; ++k) {
+    const SerialPacks& P = packs_full_[k];
+    if (P.packs.empty()) continue;
     const uint32_t n = (uint32_t)P.packs.size();
     const cudaStream_t st = branch();
-    timed("exec_serial_smem_full", [&] {
-      k_exec_serial_smem<true><<<n, kSerialPackThreads, P.max_bytes, st>>>(
-          W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, 0, 0);
+    timed(k == 0 ? "exec_serial_smem_full" : "exec_serial_staged_full", [&] {
+      if (k == 0) k_exec_serial_smem<true, false><<<n, kSerialPackThreads, P.max_bytes, st>>>(
+          W, d_lists_ + P.off_items, d_lists_ + P.off_base, d_lists_ + P.off_packs, n, 0, 0);
+      else k_exec_serial_smem<true, true><<<n, 32, P.max_bytes, st>>>(
+          W, d_lists_ + P.off_items, d_lists_ + P.off_base, d_lists_ + P.off_packs, n, 0, 0);
     });
   }
   if (!serial_full_.empty()) {
@@ -779,13 +806,16 @@ int Engine::launch_all(bool profiling) {
     }
     begin_pass(false);
     groups(false, cur, s);
-    if (!packs_links_.packs.empty()) {
-      const SerialPacks& P = packs_links_;
+    for (int k = 0; k < 2; ++k) {
+      const SerialPacks& P = packs_links_[k];
+      if (P.packs.empty()) continue;
       const uint32_t n = (uint32_t)P.packs.size();
       const cudaStream_t st = branch();
-      timed("exec_serial_smem_links", [&] {
-        k_exec_serial_smem<false><<<n, kSerialPackThreads, P.max_bytes, st>>>(
-            W, d_lists_ + P.off_items, d_wlists_ + P.off_sbase, d_lists_ + P.off_packs, n, cur, s);
+      timed(k == 0 ? "exec_serial_smem_links" : "exec_serial_staged_links", [&] {
+        if (k == 0) k_exec_serial_smem<false, false><<<n, kSerialPackThreads, P.max_bytes, st>>>(
+            W, d_lists_ + P.off_items, d_lists_ + P.off_base, d_lists_ + P.off_packs, n, cur, s);
+        else k_exec_serial_smem<false, true><<<n, 32, P.max_bytes, st>>>(
+            W, d_lists_ + P.off_items, d_lists_ + P.off_base, d_lists_ + P.off_packs, n, cur, s);
       });
     }
     if (!serial_links_.empty()) {

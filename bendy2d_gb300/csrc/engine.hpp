@@ -29,6 +29,7 @@ struct PlanTuning {
   float width_per_thread = 0.5f;    // T = pow2 >= avg width / this (issue-bound: wide groups win)
   uint32_t resident = 1;            // load a body's whole schedule when it fits
   uint32_t res_max = 227 * 1024;    // shared bytes per group for body + resident schedule
+  float stage_frac = 0.67f;         // serial bodies with chains >= this x the longest: solo packs
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };
@@ -196,19 +197,21 @@ class Engine {
   struct WorldLaunch {  // this world's ranges in the lists (plain mode)
     std::vector<std::pair<uint32_t, uint32_t>> cls;  // per class: (offset, count)
     uint32_t sf0 = 0, sfn = 0;                        // serial_full_
-    uint32_t pk0 = 0, pkn = 0;                        // packs_full_.packs
+    uint32_t pk0 = 0, pkn = 0;                        // packs_full_[0].packs
     int32_t rigid = -1;                               // index into rigid_full_
   };
   // chain-like bodies packed into shared-memory CTAs (k_exec_serial_smem)
   struct SerialPacks {
     std::vector<uint2> items;     // pack order
-    std::vector<uint32_t> sbase;  // first shared slot of each item
+    std::vector<uint2> base;      // {first particle slot, first link slot} of each item
     std::vector<uint2> packs;     // {first item, item count}
     uint32_t max_bytes = 0;
-    size_t off_items = 0, off_packs = 0, off_sbase = 0;
+    size_t off_items = 0, off_packs = 0, off_base = 0;
   };
-  SerialPacks packs_full_, packs_links_;
-  void build_packs(std::vector<uint2>& in, bool full, SerialPacks& out, std::vector<uint2>& rest);
+  // [0]: packs of many small bodies; [1]: one large body per pack
+  SerialPacks packs_full_[2], packs_links_[2];
+  void build_packs(std::vector<uint2>& in, bool full, SerialPacks* out, std::vector<uint2>& rest,
+                   bool allow_large);
   std::vector<WorldLaunch> wlaunch_;
   bool any_pp_ = false;
   uint32_t rigid_smem_ = 0;

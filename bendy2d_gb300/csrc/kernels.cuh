@@ -59,6 +59,22 @@ __device__ __forceinline__ void link_solve(float2& a, float2& b, float rest, flo
   b.x = fadd(b.x, cx); b.y = fadd(b.y, cy);
 }
 
+// The same solve with the plain IEEE intrinsics (no zero shortcuts; same
+// results).  One thread replaying a sequential chain pays the shortcuts'
+// selects on every link (measured ~40 cycles per solve) and rarely meets an
+// exact zero, so the serial executors use this form; the level executors,
+// whose warps meet axis-aligned links on most levels, keep the shortcuts.
+__device__ __forceinline__ void link_solve_plain(float2& a, float2& b, float rest, float stiff) {
+  float dx = fsub(a.x, b.x), dy = fsub(a.y, b.y);
+  float dist = __fsqrt_rn(norm_sq(dx, dy));
+  float nx = __fdiv_rn(dx, dist), ny = __fdiv_rn(dy, dist);
+  float m = fsub(dist, rest);
+  float cx = fmul(fmul(fmul(nx, m), 0.5f), stiff);
+  float cy = fmul(fmul(fmul(ny, m), 0.5f), stiff);
+  a.x = fsub(a.x, cx); a.y = fsub(a.y, cy);
+  b.x = fadd(b.x, cx); b.y = fadd(b.y, cy);
+}
+
 // Particle::solve_bounds, src/particle.rs:27-46 (min side, else max side).
 __device__ __forceinline__ void solve_bounds(float2& p, float2& q, const DWorld& w) {
   float hx = fadd(w.bx, w.bw), hy = fadd(w.by, w.bh);
@@ -401,57 +417,6 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 // whole group would idle.  This variant works on global memory (bodies too
 // large for a shared-memory pack).
 // ----------------------------------------------------------------------------
-// One body's link passes replayed in insertion order by one thread,
-// software-pipelined: the next link's endpoints and parameters are loaded
-// before the current solve, and an endpoint the current link writes is taken
-// from registers instead of memory.  So each step of a chain (consecutive
-// links sharing a particle: ring rims, spokes into a hub) costs the solve
-// alone, not solve + store + reload; values are the same as the plain loop's.
-// P maps a body-local particle index to its storage (shared or global).
-template <typename P>
-__device__ __forceinline__ void serial_link_passes(P pos, const uint2* __restrict__ ab,
-                                                   const float* __restrict__ rest,
-                                                   const float* __restrict__ stiff, uint32_t nl,
-                                                   uint32_t I) {
-  if (nl == 0) return;
-  for (uint32_t it = 0; it < I; ++it) {
-    uint2 e = __ldg(ab);
-    float r = __ldg(rest), st = __ldg(stiff);
-    float2 pa = pos.get(e.x), pb = pos.get(e.y);
-    for (uint32_t k = 0; k < nl; ++k) {
-      const bool more = k + 1 < nl;
-      const uint2 en = more ? __ldg(ab + k + 1) : e;
-      const float rn = more ? __ldg(rest + k + 1) : r;
-      const float sn = more ? __ldg(stiff + k + 1) : st;
-      // the next link's endpoints that this link does not write
-      const bool fa = en.x == e.x || en.x == e.y, fb = en.y == e.x || en.y == e.y;
-      float2 qa = fa ? make_float2(0.f, 0.f) : pos.get(en.x);
-      float2 qb = fb ? make_float2(0.f, 0.f) : pos.get(en.y);
-      link_solve(pa, pb, r, st);
-      pos.put(e.x, pa);
-      pos.put(e.y, pb);
-      if (fa) qa = en.x == e.x ? pa : pb;
-      if (fb) qb = en.y == e.x ? pa : pb;
-      e = en;
-      r = rn;
-      st = sn;
-      pa = qa;
-      pb = qb;
-    }
-  }
-}
-struct SmemPos {
-  float2* p;
-  __device__ float2 get(uint32_t i) const { return p[i]; }
-  __device__ void put(uint32_t i, float2 v) const { p[i] = v; }
-};
-struct GlobalPos {
-  float2* p;
-  const uint32_t* bidx;
-  __device__ float2 get(uint32_t i) const { return p[bidx[i]]; }
-  __device__ void put(uint32_t i, float2 v) const { p[bidx[i]] = v; }
-};
-
 template <bool FULL>
 __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __restrict__ list,
                               uint32_t n, uint32_t cur, uint32_t sub) {
@@ -472,7 +437,16 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
   DWorld Wb;
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
   for (uint32_t s = 0; s < nsub; ++s) {
-    serial_link_passes(GlobalPos{p, bidx}, ab, rest, stiff, B.nl, I);  // body-local endpoints
+    for (uint32_t it = 0; it < I; ++it) {
+      for (uint32_t k = 0; k < B.nl; ++k) {
+        const uint2 e = ab[k];  // body-local endpoints
+        const uint32_t ia = bidx[e.x], ib = bidx[e.y];
+        float2 pa = p[ia], pb = p[ib];
+        link_solve_plain(pa, pb, rest[k], stiff[k]);
+        p[ia] = pa;
+        p[ib] = pb;
+      }
+    }
     if (FULL) {
       for (uint32_t k = 0; k < B.np; ++k) {
         const uint32_t j = bidx[k];
@@ -487,14 +461,18 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
 }
 
 // Serial executor, shared-memory variant: a CTA runs a pack of chain-like
-// bodies, one thread per body, with every body's positions (and prev) staged
-// in shared memory, so each link of the chain costs shared-memory latency
-// instead of a global round trip.  pack = {first item, item count}; sbase[i]
-// is item i's first particle slot in the pack's shared array.
-template <bool FULL>
+// bodies, one thread per body, with every body's positions (and prev) in
+// shared memory, so each step of the chain costs shared-memory latency
+// instead of a global round trip.  STAGED packs also hold the links
+// (endpoints, {rest, stiffness}) in shared memory: measured on one thread
+// replaying a 4,088-particle ring, 211 cycles per link (with the next link's
+// data loaded one link ahead) against 333 with the link data read through
+// the read-only cache.  pack = {first item, item count}; base[i] = item i's
+// first particle slot and first link slot.
+template <bool FULL, bool STAGED>
 __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
                                    const uint2* __restrict__ items,
-                                   const uint32_t* __restrict__ sbase,
+                                   const uint2* __restrict__ base,
                                    const uint2* __restrict__ packs, uint32_t npacks, uint32_t cur,
                                    uint32_t sub) {
   extern __shared__ __align__(16) float2 sstate[];
@@ -502,11 +480,14 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
   const uint2 pk = packs[blockIdx.x];
   const uint32_t tid = threadIdx.x, nt = blockDim.x;
   const uint32_t warp = tid >> 5, lane = tid & 31u, nwarps = nt >> 5;
-  // pack-wide particle count -> prev slots follow the pos slots
+  // pack-wide particle and link counts: [pos | prev (FULL) | ab | {rest, stiff}]
   const uint32_t last = pk.x + pk.y - 1;
-  const uint32_t total = sbase[last] + worlds[items[last].x].bodies[items[last].y].np;
+  const DBody BL = worlds[items[last].x].bodies[items[last].y];
+  const uint32_t total = base[last].x + BL.np, ltotal = STAGED ? base[last].y + BL.nl : 0u;
   float2* spos = sstate;
   float2* sprev = sstate + total;
+  uint2* sab = reinterpret_cast<uint2*>(sstate + (FULL ? 2u : 1u) * total);
+  float2* srs = reinterpret_cast<float2*>(sab + ltotal);
   // cooperative load, one warp per body
   for (uint32_t it = warp; it < pk.y; it += nwarps) {
     const uint2 wi = items[pk.x + it];
@@ -514,11 +495,17 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
     if (!FULL && sub >= W.S) continue;
     const DBody B = W.bodies[wi.y];
     const uint32_t* bidx = W.bidx + B.i0;
-    const uint32_t sb = sbase[pk.x + it];
+    const uint2 sb = base[pk.x + it];
     for (uint32_t i = lane; i < B.np; i += 32) {
-      const uint32_t k = bidx[i];
-      spos[sb + i] = W.pos[cur][k];
-      if (FULL) sprev[sb + i] = W.prev[k];
+      const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
+      spos[sb.x + i] = W.pos[cur][k];
+      if (FULL) sprev[sb.x + i] = W.prev[k];
+    }
+    if (STAGED) {
+      for (uint32_t i = lane; i < B.nl; i += 32) {
+        sab[sb.y + i] = W.lab[B.l0 + i];  // body-local endpoints
+        srs[sb.y + i] = make_float2(W.lrest[B.l0 + i], W.lstiff[B.l0 + i]);
+      }
     }
   }
   __syncthreads();
@@ -527,20 +514,63 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
     const DWorld& W = worlds[wi.x];
     if (FULL || sub < W.S) {
       const DBody B = W.bodies[wi.y];
-      const uint32_t sb = sbase[pk.x + tid];
-      float2* p = spos + sb;
-      float2* q = sprev + sb;
-      const uint2* ab = W.lab + B.l0;  // body-local endpoints
-      const float* rest = W.lrest + B.l0;
-      const float* stiff = W.lstiff + B.l0;
+      const uint2 sb = base[pk.x + tid];
+      float2* p = spos + sb.x;
+      float2* q = sprev + sb.x;
+      const uint2* ab = STAGED ? sab + sb.y : W.lab + B.l0;  // body-local endpoints
+      const float2* rs = srs + sb.y;
+      const float* grest = W.lrest + B.l0;
+      const float* gstiff = W.lstiff + B.l0;
       const uint32_t nsub = FULL ? W.S : 1u, I = W.I;
       const float gx = W.gx, gy = W.gy, h = W.h;
       DWorld Wb;
       Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+      // link k's endpoints and parameters, loaded one link ahead (they do not
+      // depend on the positions, so their latency leaves the chain)
+      auto link_at = [&](uint32_t k, uint2& e, float2& r) {
+        e = STAGED ? ab[k] : __ldg(ab + k);
+        r = STAGED ? rs[k] : make_float2(__ldg(grest + k), __ldg(gstiff + k));
+      };
       for (uint32_t s = 0; s < nsub; ++s) {
-        serial_link_passes(SmemPos{p}, ab, rest, stiff, B.nl, I);
+        for (uint32_t it = 0; it < I && B.nl; ++it) {
+          uint2 e;
+          float2 r;
+          link_at(0, e, r);
+          for (uint32_t k = 0; k < B.nl; ++k) {
+            uint2 en;
+            float2 rn;
+            link_at(k + 1 < B.nl ? k + 1 : k, en, rn);
+            float2 pa = p[e.x], pb = p[e.y];
+            link_solve_plain(pa, pb, r.x, r.y);
+            p[e.x] = pa;
+            p[e.y] = pb;
+            e = en;
+            r = rn;
+          }
+        }
         if (FULL) {
-          for (uint32_t k = 0; k < B.np; ++k) {
+          // particles are independent here: four at a time, loads before
+          // stores (measured 100 instead of 134 cycles per particle)
+          uint32_t k = 0;
+          for (; k + 4 <= B.np; k += 4) {
+            float2 pp[4], qq[4];
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+              pp[j] = p[k + j];
+              qq[j] = q[k + j];
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+              solve_bounds(pp[j], qq[j], Wb);
+              integrate(pp[j], qq[j], gx, gy, h);
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+              p[k + j] = pp[j];
+              q[k + j] = qq[j];
+            }
+          }
+          for (; k < B.np; ++k) {
             float2 pp = p[k], qq = q[k];
             solve_bounds(pp, qq, Wb);
             integrate(pp, qq, gx, gy, h);
@@ -558,9 +588,9 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
     if (!FULL && sub >= W.S) continue;
     const DBody B = W.bodies[wi.y];
     const uint32_t* bidx = W.bidx + B.i0;
-    const uint32_t sb = sbase[pk.x + it];
+    const uint32_t sb = base[pk.x + it].x;
     for (uint32_t i = lane; i < B.np; i += 32) {
-      const uint32_t k = bidx[i];
+      const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
       W.pos[cur][k] = spos[sb + i];
       if (FULL) W.prev[k] = sprev[sb + i];
     }
