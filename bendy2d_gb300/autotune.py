@@ -8,6 +8,9 @@ updates after warm-up) and the fastest kept.  Tunables:
   t_max             largest group size
   max_groups        groups per CTA for T > 32 (1 spreads bodies over SMs)
   serial_width      schedule width below which a body runs serially
+  resident          hold a body's whole schedule in shared memory when it fits
+  stage_frac        serial bodies with chains >= this x the longest run alone,
+                    links staged in shared memory
 Results are cached in memory by a scene signature.
 """
 from __future__ import annotations
@@ -20,6 +23,8 @@ SPACE = {
     "t_max": [128, 256, 512],
     "max_groups": [1, 2],
     "serial_width": [1.5, 2.0, 4.0],
+    "resident": [0, 1],
+    "stage_frac": [0.4, 0.67, 1.01],
 }
 _CACHE: dict = {}
 
