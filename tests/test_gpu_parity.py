@@ -369,3 +369,42 @@ def test_config5_full_size_isolated_bodies_match_oracle(gpu):
     gc = s.get_circles()
     oc, _ = o.circles()
     assert same_bits([c.point.pos for c in gc], oc)
+
+
+@pytest.mark.parametrize("tuning", [
+    {"t_max": 64}, {"t_min": 256, "t_max": 256}, {"width_per_thread": 2.0},
+    {"resident": 0}, {"serial_width": 1000.0}, {"serial_width": 0.0},
+    {"max_groups": 1, "warp_groups": 1}, {"stage_frac": 0.0}, {"stage_frac": 2.0},
+    {"smem_max": 16384},
+])
+def test_tunables_never_change_results(gpu, tuning):
+    """Executor tunables move work between executors, group sizes, launch
+    classes and pack kinds; the bits must stay those of the defaults."""
+    from bendy2d_gb300 import Batch, scenes
+    rng = np.random.default_rng(51)
+    worlds = [scenes.config2(seed=11, n_bodies=4, box=110.0, n_circles=3, n_polys=2),
+              scenes.config3_world(rng, 900, link_iters=2), scenes.config1(seed=6)]
+    ref = [w.to_solver() for w in worlds]
+    tuned = [w.to_solver() for w in worlds]
+    bref, btun = Batch(ref), Batch(tuned)
+    btun.set_tuning(**tuning)
+    for _ in range(3):
+        bref.update(worlds[0].dt)
+        btun.update(worlds[0].dt)
+    for a, b in zip(ref, tuned):
+        assert_same_state(solver_state(a), solver_state(b), f"tuning {tuning}")
+    bref.close()
+    btun.close()
+
+
+def test_autotune_returns_a_valid_tuning(gpu):
+    from bendy2d_gb300 import autotune, scenes
+    sc = scenes.config2(seed=12, n_bodies=2, box=80.0, n_circles=2, n_polys=1)
+    best = autotune.autotune(sc, steps=1, warmup=1, space={"t_max": [128, 256], "resident": [0, 1]})
+    knobs = {k: v for k, v in best.items() if not k.startswith("_")}
+    assert set(knobs) <= {"t_max", "resident"}
+    assert best.get("_ms_per_step", 1.0) > 0.0
+    s = sc.to_solver()
+    if knobs:
+        s.set_tuning(**knobs)
+    s.update(sc.dt)
