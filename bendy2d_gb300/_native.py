@@ -52,7 +52,8 @@ class CNoAllocParams(C.Structure):
 class CServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "admitted", "completed", "failed",
                                           "queued", "active", "ticks", "particle_substeps",
-                                          "resident_bytes")]
+                                          "resident_bytes", "admit_ns", "step_ns",
+                                          "retire_ns")]
 
 
 class CPlanStats(C.Structure):

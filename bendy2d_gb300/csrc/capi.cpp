@@ -792,6 +792,9 @@ int b2d_server_get_stats(b2d_server* sv, b2d_server_stats* out) {
   out->ticks = s.ticks;
   out->particle_substeps = s.particle_substeps;
   out->resident_bytes = s.resident_bytes;
+  out->admit_ns = s.admit_ns;
+  out->step_ns = s.step_ns;
+  out->retire_ns = s.retire_ns;
   return OK;
 }
 

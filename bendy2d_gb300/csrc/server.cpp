@@ -172,6 +172,7 @@ void Server::loop() {
       }
     }
     if (!eng) eng = std::make_unique<Engine>(nullptr);
+    const Clock::time_point ta = Clock::now();
     for (Req* r : admit) {
       std::string why;
       int st = eng->add(&r->world, &r->slot, &why);
@@ -191,9 +192,11 @@ void Server::loop() {
       ++stats_.admitted;
     }
     std::vector<Req*> act;
+    const Clock::time_point ts = Clock::now();
     {
       std::lock_guard<std::mutex> lk(mu_);
       act = active_;
+      stats_.admit_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(ts - ta).count();
     }
     if (act.empty()) continue;
     // requests that asked for zero steps finish without a tick
@@ -204,6 +207,7 @@ void Server::loop() {
       st = eng->step();
       if (st == OK) st = eng->sync();
     }
+    const Clock::time_point tr = Clock::now();
     uint64_t units = 0;
     std::vector<Req*> finished;
     for (Req* r : act) {
@@ -230,9 +234,12 @@ void Server::loop() {
       active_.erase(std::find(active_.begin(), active_.end(), r));
       finished_.push_back(r->id);
     }
+    const Clock::time_point te = Clock::now();
     std::lock_guard<std::mutex> lk(mu_);
     ++stats_.ticks;
     stats_.particle_substeps += units;
+    stats_.step_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(tr - ts).count();
+    stats_.retire_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(te - tr).count();
   }
   eng.reset();
 }

@@ -21,6 +21,7 @@ struct ServerStats {
   uint64_t queued = 0, active = 0;
   uint64_t ticks = 0, particle_substeps = 0;
   uint64_t resident_bytes = 0;
+  uint64_t admit_ns = 0, step_ns = 0, retire_ns = 0;  // worker wall time per phase
 };
 
 class Server {

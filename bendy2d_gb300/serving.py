@@ -145,4 +145,6 @@ def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
         "throughput_particle_substeps_per_s": stats["particle_substeps"] / wall,
         "completed_particle_substeps_per_s": done_units / wall,
         "ticks": stats["ticks"], "budget_bytes": budget_bytes,
+        "worker_s": {"admit": stats["admit_ns"] / 1e9, "step": stats["step_ns"] / 1e9,
+                     "retire": stats["retire_ns"] / 1e9},
     }

@@ -215,6 +215,9 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
 typedef struct {
   uint64_t submitted, admitted, completed, failed, queued, active;
   uint64_t ticks, particle_substeps, resident_bytes;
+  /* worker wall time, nanoseconds: admitting (planning + upload), stepping
+   * (launch + wait), retiring (download + release) */
+  uint64_t admit_ns, step_ns, retire_ns;
 } b2d_server_stats;
 int b2d_server_create(uint64_t budget_bytes, b2d_server** out);
 int b2d_server_destroy(b2d_server* sv);
