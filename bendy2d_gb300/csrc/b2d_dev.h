@@ -22,7 +22,6 @@ enum : uint32_t { COLLIDE_PP = 1u, COLLIDE_PC = 2u, COLLIDE_PPOLY = 4u };
 // integrate ops carry the body-local particle index with this bit set.
 constexpr uint32_t OP_INTEG = 0x80000000u;
 constexpr uint32_t OP_WIDE = 0xFFFFFFFFu;
-constexpr uint32_t OP_NONE = 0xFFFFFFFEu;  // executor-internal: no op
 
 // A body is a set of solver particles run by one executor unit: a union of
 // whole link-connected components, so no link crosses two bodies.
