@@ -11,6 +11,7 @@ updates after warm-up) and the fastest kept.  Tunables:
   resident          hold a body's whole schedule in shared memory when it fits
   stage_frac        serial bodies with chains >= this x the longest run alone,
                     links staged in shared memory
+  bucket_factor     collision-grid buckets per world: pow2 >= this x particles
 Results are cached in memory by a scene signature.
 """
 from __future__ import annotations
@@ -25,6 +26,7 @@ SPACE = {
     "serial_width": [1.5, 2.0, 4.0],
     "resident": [0, 1],
     "stage_frac": [0.4, 0.67, 1.01],
+    "bucket_factor": [1.0, 2.0, 4.0],
 }
 _CACHE: dict = {}
 

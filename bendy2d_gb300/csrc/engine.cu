@@ -115,9 +115,10 @@ void Engine::set_stream(cudaStream_t s) {
 }
 
 void Engine::set_tuning(const PlanTuning& t) {
-  const uint32_t cap = tune_.smem_max;
+  const uint32_t cap = tune_.smem_max, rcap = tune_.res_max;
   tune_ = t;
-  tune_.smem_max = std::min(tune_.smem_max, cap);
+  tune_.smem_max = std::min(tune_.smem_max, cap);  // device limits found at start-up
+  tune_.res_max = std::min(tune_.res_max, rcap);
   lists_dirty_ = true;
 }
 
@@ -536,7 +537,8 @@ int Engine::rebuild_lists() {
       if (im.params.flags & COLLIDE_PP) {
         any_pp_ = true;
         // this world's bucket range: a power of two >= 2 x its particles
-        const uint32_t nbw = pow2ceil_u(std::max<uint32_t>(2u * im.params.np, 64u));
+        const uint32_t nbw = pow2ceil_u(std::max<uint32_t>(
+            (uint32_t)(tune_.bucket_factor * (float)im.params.np), 64u));
         if (h_worlds_[si].gb0 != (uint32_t)nbuckets || h_worlds_[si].gmask != nbw - 1 ||
             h_worlds_[si].gp0 != (uint32_t)np_pp) {
           h_worlds_[si].gb0 = (uint32_t)nbuckets;

@@ -30,6 +30,7 @@ struct PlanTuning {
   uint32_t resident = 1;            // load a body's whole schedule when it fits
   uint32_t res_max = 227 * 1024;    // shared bytes per group for body + resident schedule
   float stage_frac = 0.67f;         // serial bodies with chains >= this x the longest: solo packs
+  float bucket_factor = 2.0f;       // collision-grid buckets per world: pow2 >= this x particles
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };

@@ -41,6 +41,7 @@ bool PlanTuning::set(const std::string& k, double v) {
   else if (k == "resident") resident = (uint32_t)v;
   else if (k == "res_max") res_max = (uint32_t)v;
   else if (k == "stage_frac") stage_frac = (float)v;
+  else if (k == "bucket_factor") bucket_factor = (float)v;
   else return false;
   return true;
 }
