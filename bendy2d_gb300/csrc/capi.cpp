@@ -598,9 +598,8 @@ int b2d_get_plan_stats(b2d_solver* s, b2d_plan_stats* out) {
     int st = sync_host(s);
     if (st != OK) return st;
     SchedRegistry reg;
-    PlanTuning tune;
     std::string why;
-    st = plan_world(s->w, tune, reg, tmp, &why);
+    st = plan_world(s->w, s->tune, reg, tmp, &why);  // the solver's own tunables
     if (st != OK) return fail(st, why);
     im = &tmp;
   } else {

@@ -163,3 +163,39 @@ def test_fast_mode_colouring_is_proper(native_lib):
     # fast mode needs far fewer levels than reference order
     ref = scenes.config1(steps=1).to_solver().plan_stats()
     assert st["levels"] < ref["levels"]
+
+
+def test_plan_config2_links_only_levels(native_lib):
+    """With particle collisions on, each sub-step's 4 link passes form their
+    own schedule: 153 levels for every 32x32 cloth (64 bodies)."""
+    from bendy2d_gb300 import scenes
+    st = scenes.config2(seed=0).to_solver().plan_stats()
+    assert st["group_bodies"] == 64 and st["serial_bodies"] == 0
+    assert st["levels"] == 64 * 153
+    assert st["ops"] == 64 * 4 * 3906
+
+
+def test_tunables_move_bodies_between_executors(native_lib):
+    """serial_width decides group vs serial execution; smem_max pushes bodies
+    to the global-memory executor; the plan still covers every link."""
+    from bendy2d_gb300 import scenes
+    sc = scenes.config2(seed=1, n_bodies=3, box=100.0, n_circles=1, n_polys=1)
+    s = sc.to_solver()
+    base = s.plan_stats()
+    s.set_tuning(serial_width=1e9)
+    ser = s.plan_stats()
+    assert ser["serial_bodies"] == base["group_bodies"] + base["serial_bodies"]
+    assert ser["group_bodies"] == 0
+    s2 = sc.to_solver()
+    s2.set_tuning(smem_max=1024)
+    glob = s2.plan_stats()
+    assert glob["global_bodies"] == glob["group_bodies"] == base["group_bodies"]
+    assert glob["ops"] == base["ops"]
+
+
+def test_unknown_tunable_is_rejected(native_lib):
+    from bendy2d_gb300 import B2DError, Solver
+    s = Solver()
+    with pytest.raises(B2DError) as e:
+        s.set_tuning(no_such_knob=1.0)
+    assert "unknown tunable" in str(e.value)
