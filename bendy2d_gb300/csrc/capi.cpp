@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -51,6 +52,7 @@ struct b2d_server {
 };
 
 struct b2d_batch {
+  std::recursive_mutex mu;  // every b2d_batch_* call holds it
   std::unique_ptr<Engine> eng;
   std::vector<b2d_solver*> members;
   cudaStream_t stream = nullptr;
@@ -635,12 +637,16 @@ int b2d_batch_create(b2d_batch** out) {
 }
 int b2d_batch_destroy(b2d_batch* b) {
   if (!b) return OK;
-  while (!b->members.empty()) b2d_batch_remove(b, b->members.back());
+  {
+    std::lock_guard<std::recursive_mutex> lk(b->mu);
+    while (!b->members.empty()) b2d_batch_remove(b, b->members.back());
+  }
   delete b;
   return OK;
 }
 int b2d_batch_add(b2d_batch* b, b2d_solver* s) {
   if (!b || !s) return fail(ERR_NULL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   if (s->batch) return fail(ERR_STATE, "solver already belongs to a batch");
   int st = unplace(s);
   if (st != OK) return st;
@@ -650,6 +656,7 @@ int b2d_batch_add(b2d_batch* b, b2d_solver* s) {
 }
 int b2d_batch_remove(b2d_batch* b, b2d_solver* s) {
   if (!b || !s) return fail(ERR_NULL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   auto it = std::find(b->members.begin(), b->members.end(), s);
   if (it == b->members.end()) return fail(ERR_STATE, "solver is not in this batch");
   int st = unplace(s);
@@ -661,6 +668,7 @@ int b2d_batch_remove(b2d_batch* b, b2d_solver* s) {
 }
 int b2d_batch_update(b2d_batch* b, float dt) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   for (b2d_solver* s : b->members) {
     int st = ensure_placed(s);
     if (st != OK) return st;
@@ -676,28 +684,33 @@ int b2d_batch_update(b2d_batch* b, float dt) {
 }
 int b2d_batch_synchronize(b2d_batch* b) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   if (!b->eng) return OK;
   int st = b->eng->sync();
   return st == OK ? OK : fail(st, b->eng->last_error);
 }
 int b2d_batch_set_stream(b2d_batch* b, void* stream) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   b->stream = static_cast<cudaStream_t>(stream);
   if (b->eng) b->eng->set_stream(b->stream);
   return OK;
 }
 int b2d_batch_set_profiling(b2d_batch* b, int on) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   b->profiling = on != 0;
   return OK;
 }
 int b2d_batch_get_profile(b2d_batch* b, char* names, size_t names_cap, float* ms, size_t cap,
                           size_t* count) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   return put_profile(b->eng.get(), names, names_cap, ms, cap, count);
 }
 int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value) {
   if (!b || !key) return fail(ERR_NULL, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   if (!b->tune.set(key, value)) return fail(ERR_ARG, std::string("unknown tunable: ") + key);
   b->tune_set = true;
   if (b->eng) {
@@ -711,12 +724,14 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value) {
 }
 int b2d_batch_set_plain(b2d_batch* b, int on) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   b->plain = on != 0;
   if (b->eng) b->eng->set_plain(b->plain);
   return OK;
 }
 int b2d_batch_get_launch_count(b2d_batch* b, uint32_t* out) {
   if (!b) return fail(ERR_NULL, "null batch");
+  std::lock_guard<std::recursive_mutex> lk(b->mu);
   *out = b->eng ? b->eng->launches_per_step() : 0;
   return OK;
 }

@@ -6,7 +6,10 @@
  * gives a message for the last failure on the calling thread.  The caller
  * owns host buffers; the library owns device memory.  A solver is used from
  * one thread at a time (the reference's update takes &mut self,
- * src/solver.rs:106); batches and servers synchronise internally.
+ * src/solver.rs:106).  Batch calls hold the batch's lock, so several threads
+ * may call b2d_batch_* on one batch; calls on a member solver share the
+ * batch's engine and must not overlap batch calls.  Servers synchronise
+ * internally.
  *
  * Reference citations are file:line within the bendy2d crate (src/...).
  */

@@ -408,3 +408,36 @@ def test_autotune_returns_a_valid_tuning(gpu):
     if knobs:
         s.set_tuning(**knobs)
     s.update(sc.dt)
+
+
+def test_batch_updates_from_two_threads(gpu):
+    """Batch calls hold the batch's lock: two threads updating one batch
+    concurrently give exactly two steps."""
+    import threading
+    from bendy2d_gb300 import Batch, scenes
+    rng = np.random.default_rng(61)
+    worlds = [scenes.config3_world(rng, int(n)) for n in (200, 700, 1300)]
+    worlds.append(scenes.config2(seed=13, n_bodies=2, box=90.0, n_circles=2, n_polys=1))
+    alone = [w.to_solver() for w in worlds]
+    shared = [w.to_solver() for w in worlds]
+    b = Batch(shared)
+    errs = []
+
+    def one():
+        try:
+            b.update(worlds[0].dt)
+        except Exception as e:  # surfaced below
+            errs.append(e)
+
+    th = [threading.Thread(target=one) for _ in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errs, errs
+    for s, w in zip(alone, worlds):
+        s.update(w.dt)
+        s.update(w.dt)
+    for a, t in zip(alone, shared):
+        assert_same_state(solver_state(a), solver_state(t), "two threads")
+    b.close()
