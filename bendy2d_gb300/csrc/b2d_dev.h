@@ -13,6 +13,8 @@
 #include <vector_functions.h>
 #include <vector_types.h>
 
+#include <cstring>
+
 namespace b2d {
 
 // Collision extension flags (not in the reference; see solve_dynamic_collisions).
@@ -65,6 +67,21 @@ struct DSched {
   uint32_t len0, pad;        // words of the first chunk
 };
 
+// 1 / c when c is a positive normal power of two (then x / c == x * (1/c)
+// exactly for every x: both round the same real number), else 0.
+inline float pow2_reciprocal(float c) {
+  uint32_t u;
+  std::memcpy(&u, &c, 4);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if ((u >> 31) || (u & 0x7FFFFFu) || e == 0u || e == 255u) return 0.0f;
+  const int ne = 254 - (int)e;  // 2^(127 - (e - 127)) has exponent field 254 - e
+  if (ne < 1 || ne > 254) return 0.0f;
+  const uint32_t r = (uint32_t)ne << 23;
+  float f;
+  std::memcpy(&f, &r, 4);
+  return f;
+}
+
 struct DWorld {
   // parameters
   float gx, gy;          // 0 + gravity: the acceleration at integrate time
@@ -76,7 +93,8 @@ struct DWorld {
   uint32_t slot;         // stable id (hash salt for the shared grid)
   uint32_t np, nb, nc, ncl, ng;
   uint32_t gb0, gmask;   // extension grid: this world's buckets [gb0, gb0 + gmask]
-  uint32_t gp0, pad;     // extension grid: this world's particle scratch offset
+  uint32_t gp0;          // extension grid: this world's particle scratch offset
+  float icell;           // 1 / cell when cell is a power of two (exact), else 0
   // solver particles
   float2* pos[2];        // ping-pong positions; pos[0] holds the state between steps
   float2* prev;

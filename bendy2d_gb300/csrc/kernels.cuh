@@ -1079,8 +1079,12 @@ __global__ void __launch_bounds__(256) k_rigid(const DWorld* __restrict__ worlds
 // particle of the 9 surrounding cells, summed in fixed point so that the
 // result does not depend on the visiting order.
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell) {
-  float v = floorf(fdiv(fsub(p, origin), cell));
+// Cell index along one axis: floor((p - origin) / cell), clamped.  For a
+// power-of-two cell the division is the multiplication by icell (exact, the
+// same bits); otherwise icell is 0 and the IEEE division runs.
+__device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell, float icell) {
+  const float t = fsub(p, origin);
+  float v = floorf(icell != 0.0f ? fmul(t, icell) : fdiv(t, cell));
   if (!(v > -1.0e9f)) v = -1.0e9f;
   if (v > 1.0e9f) v = 1.0e9f;
   return (int32_t)v;
@@ -1115,7 +1119,7 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   const uint32_t j = ch.y + threadIdx.x;
   if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
   const float2 p = W.pos[cur][j];
-  const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
   const uint32_t b = bucket_of(W, cx, cy);
   const uint32_t r = atomicAdd(&G.count[b], 1u);
   G.pbr[W.gp0 + j] = make_uint2(b, r);
@@ -1326,7 +1330,7 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
   if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
   const float2 p = W.pos[cur][j];
   const uint2 br = G.pbr[W.gp0 + j];
-  const int32_t cx = cell_coord(p.x, W.bx, W.cell), cy = cell_coord(p.y, W.by, W.cell);
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
   G.sorted[G.range[br.x].x + br.y] =
       make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), (uint32_t)cx, (uint32_t)cy);
 }
@@ -1502,8 +1506,8 @@ static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
     long long sx = 0, sy = 0;
     bool hit = false;
     if (act && lane < 3) {
-      const int32_t cx = cell_coord(p.x, W.bx, W.cell);
-      const int32_t cy = cell_coord(p.y, W.by, W.cell) + (int32_t)lane - 1;  // this lane's row
+      const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell);
+      const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell) + (int32_t)lane - 1;  // this lane's row
       const float D = fadd(W.radius, W.radius);
       const float D2 = fmul(D, D);
       const uint32_t b0 = bucket_of(W, cx - 1, cy), b1 = bucket_of(W, cx, cy),

@@ -125,6 +125,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   w.h = p->dt * (1.0f / (float)p->sub_steps);  // src/solver.rs:107-108
   w.radius = p->particle_radius;
   w.cell = p->grid_cell;
+  w.icell = pow2_reciprocal(p->grid_cell);
   w.S = p->sub_steps;
   w.I = 1;
   w.flags = COLLIDE_PP;

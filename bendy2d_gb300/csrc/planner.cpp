@@ -274,6 +274,7 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
   P.bh = w.bounds.size.y;
   P.radius = w.particle_radius;
   P.cell = w.grid_cell;
+  P.icell = pow2_reciprocal(w.grid_cell);
   P.S = w.sub_steps;
   P.I = w.link_iters;
   P.flags = w.collide & (COLLIDE_PP | COLLIDE_PC | COLLIDE_PPOLY);
