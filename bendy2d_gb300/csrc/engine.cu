@@ -850,7 +850,7 @@ int Engine::launch_all(bool profiling) {
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      k_collide_integrate<<<nch * COLLIDE_LANES, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      k_collide_integrate<<<nch * COLLIDE_CTAS, COLLIDE_THREADS, 0, stream_>>>(W, grid_, CH, nch, cur, s);
     });
     if (nre) edge(stream_, ax);
   }

@@ -1105,7 +1105,9 @@ __device__ __forceinline__ uint32_t bucket_of(const DWorld& W, int32_t cx, int32
   return W.gb0 + (((cell_hash(cx >> 2, cy) << 2) | ((uint32_t)cx & 3u)) & W.gmask);
 }
 
-constexpr uint32_t CHUNK = 256;  // particles per work chunk (one CTA)
+// particles per work chunk: one CTA of the count / scatter / copy-back
+// kernels, four collide CTAs of 8 warps x 10 particles
+constexpr uint32_t CHUNK = 320;
 
 // Bucket entry: {pos.x bits, pos.y bits, cell x, cell y}.  Cells that hash
 // to the same bucket are told apart by the stored cell coordinates, so the
@@ -1451,7 +1453,7 @@ __device__ __forceinline__ bool separated(float lo, float hi, float cmin, float 
 
 // min/max of the CTA's particle positions (NaN ignored)
 __device__ __forceinline__ float4 block_box(bool act, float2 p) {
-  __shared__ float4 wbox[CHUNK / 32];
+  __shared__ float4 wbox[32];
   float4 b = act ? make_float4(p.x, p.y, p.x, p.y)
                  : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
 #pragma unroll
@@ -1477,37 +1479,41 @@ __device__ __forceinline__ float4 block_box(bool act, float2 p) {
 // pipeline.  Reads positions from buffer cur (the post-link snapshot) and
 // writes the new ones to buffer cur^1; prev is updated in place.
 //
-// Four lanes per particle: lanes 0-2 each scan one row of the 3x3 neighbour
-// cells and the four lanes add their fixed-point sums (integer adds, so the
-// split cannot change the result); lane 0 then runs the circle and polygon
-// tests, bounds and integrate.  A CTA covers a quarter of one work chunk
-// (grid = 4 x chunks).  Circle and polygon tests are skipped for the whole
-// CTA when no circle or polygon box reaches the CTA's particles: then no
-// particle is in contact, nothing moves, and so no later test of the
-// sequence can hit either — the skip is exact.
-constexpr uint32_t COLLIDE_LANES = 4;
-static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
+// Three lanes per particle, ten particles per warp (lanes 30 and 31 idle):
+// each lane scans one row of the 3x3 neighbour cells and the owner (the
+// first lane of the three) adds their fixed-point sums (integer adds, so the
+// split cannot change the result), then runs the circle and polygon tests,
+// bounds and integrate.  A CTA of 8 warps covers 80 particles, a quarter of
+// one work chunk (grid = 4 x chunks).  Circle and polygon tests are skipped
+// for the whole CTA when no circle or polygon box reaches the CTA's
+// particles: then no particle is in contact, nothing moves, and so no later
+// test of the sequence can hit either — the skip is exact.
+constexpr uint32_t COLLIDE_THREADS = 256;      // 8 warps
+constexpr uint32_t COLLIDE_PER_WARP = 10;      // particles per warp, three lanes each
+constexpr uint32_t COLLIDE_CTAS = CHUNK / (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP);  // per chunk
+static_assert(COLLIDE_CTAS * (COLLIDE_THREADS / 32) * COLLIDE_PER_WARP == CHUNK, "chunk split");
+static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate(
     const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
-  const uint32_t cidx = blockIdx.x / COLLIDE_LANES;
+  const uint32_t cidx = blockIdx.x / COLLIDE_CTAS;
   if (cidx >= nchunks) return;
   const uint2 ch = chunks[cidx];
   const DWorld& W = worlds[ch.x];
   if (sub >= W.S) return;  // uniform over the CTA
-  const uint32_t lane = threadIdx.x % COLLIDE_LANES;
-  const uint32_t i = ch.y + (blockIdx.x % COLLIDE_LANES) * (CHUNK / COLLIDE_LANES) +
-                     threadIdx.x / COLLIDE_LANES;
-  const bool act = i < W.np;
-  const bool own = act && lane == 0;  // the lane that owns particle i
+  const uint32_t wl = threadIdx.x & 31u, grp = wl / 3u, row = wl - 3u * grp;
+  const uint32_t i = ch.y + (blockIdx.x % COLLIDE_CTAS) * (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP) +
+                     (threadIdx.x >> 5) * COLLIDE_PER_WARP + grp;
+  const bool act = grp < COLLIDE_PER_WARP && i < W.np;
+  const bool own = act && row == 0;  // the lane that owns particle i
   const float2* P = W.pos[cur];
   float2 p = act ? P[i] : make_float2(0.f, 0.f);
   float2 q = own ? W.prev[i] : make_float2(0.f, 0.f);  // issued early, used last
   if (W.flags & COLLIDE_PP) {  // uniform over the CTA
     long long sx = 0, sy = 0;
     bool hit = false;
-    if (act && lane < 3) {
+    if (act) {
       const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell);
-      const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell) + (int32_t)lane - 1;  // this lane's row
+      const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell) + (int32_t)row - 1;  // this lane's row
       const float D = fadd(W.radius, W.radius);
       const float D2 = fmul(D, D);
       const uint32_t b0 = bucket_of(W, cx - 1, cy), b1 = bucket_of(W, cx, cy),
@@ -1517,13 +1523,18 @@ static __global__ void __launch_bounds__(CHUNK, 4) k_collide_integrate(
       visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, sx, sy, hit);
       visit_cell(G, p, cx + 1, cy, r2.x, r2.y, D, D2, sx, sy, hit);
     }
-#pragma unroll
-    for (uint32_t o = 1; o < COLLIDE_LANES; o <<= 1) {
-      sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-      sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-      hit |= __shfl_xor_sync(0xFFFFFFFFu, (int)hit, o) != 0;
+    // the owner adds the other two rows' sums (lanes 30, 31 read lanes 31, 0:
+    // harmless, they own nothing)
+    const uint32_t l1 = (wl + 1u) & 31u, l2 = (wl + 2u) & 31u;
+    const long long sx1 = __shfl_sync(0xFFFFFFFFu, sx, l1), sx2 = __shfl_sync(0xFFFFFFFFu, sx, l2);
+    const long long sy1 = __shfl_sync(0xFFFFFFFFu, sy, l1), sy2 = __shfl_sync(0xFFFFFFFFu, sy, l2);
+    const int h1 = __shfl_sync(0xFFFFFFFFu, (int)hit, l1), h2 = __shfl_sync(0xFFFFFFFFu, (int)hit, l2);
+    if (own) {
+      sx += sx1 + sx2;
+      sy += sy1 + sy2;
+      hit = hit || h1 || h2;
+      if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
     }
-    if (hit) { p.x = fadd(p.x, unfix32(sx)); p.y = fadd(p.y, unfix32(sy)); }
   }
   const uint32_t flags = W.flags;
   if (flags & (COLLIDE_PC | COLLIDE_PPOLY)) {

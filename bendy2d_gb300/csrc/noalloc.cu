@@ -38,7 +38,7 @@ namespace {
 
 constexpr uint32_t NOALLOC_MAX_PARTICLES = 65536;
 constexpr uint32_t NOALLOC_MAX_BUCKETS = 2 * NOALLOC_MAX_PARTICLES;  // power of two >= 2n
-constexpr uint32_t NOALLOC_MAX_CHUNKS = NOALLOC_MAX_PARTICLES / CHUNK;
+constexpr uint32_t NOALLOC_MAX_CHUNKS = (NOALLOC_MAX_PARTICLES + CHUNK - 1) / CHUNK;
 constexpr uint32_t NOALLOC_MAX_TILES = (NOALLOC_MAX_BUCKETS + SCAN_SUB - 1) / SCAN_SUB;
 
 constexpr size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -159,7 +159,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
     k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
     k_grid_scan<1><<<nt, 1024, 0, st>>>(G, nb, nt);  // nt <= 32 one-sub-tile tiles
     k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_collide_integrate<<<nch * COLLIDE_LANES, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
+    k_collide_integrate<<<nch * COLLIDE_CTAS, COLLIDE_THREADS, 0, st>>>(dW, G, chunks, nch, cur, s);
   }
   k_copy_back<<<nch, CHUNK, 0, st>>>(dW, chunks, nch);
   cudaError_t e = cudaGetLastError();
