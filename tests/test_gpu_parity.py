@@ -441,3 +441,30 @@ def test_batch_updates_from_two_threads(gpu):
     for a, t in zip(alone, shared):
         assert_same_state(solver_state(a), solver_state(t), "two threads")
     b.close()
+
+
+def test_body_over_65535_particles_uses_wide_ops(gpu):
+    """A 260x260 cloth (67,600 particles) is one body too large for 16-bit
+    local endpoints: the global executor runs wide ops (link ids resolved
+    through the link table)."""
+    from bendy2d_gb300 import scenes
+    rng = np.random.default_rng(71)
+    body = scenes.grid_body(260, 260, (10.0, 10.0), 1.0, 0.01, rng)
+    sc = scenes._assemble("huge", [body], bounds=(0.0, 0.0, 300.0, 300.0), sub_steps=2,
+                          link_iters=1)
+    st = sc.to_solver().plan_stats()
+    assert st["global_bodies"] == 1 and st["group_bodies"] == 1
+    check(sc, 2, "wide ops")
+
+
+def test_ring_too_large_for_shared_memory_runs_serially_from_global(gpu):
+    """A hub-and-spoke ring of 9,000 rim particles: its positions alone
+    exceed a serial pack and with its links it exceeds a CTA's shared
+    memory, so the global-memory serial executor replays it."""
+    from bendy2d_gb300 import scenes
+    p, a, b = scenes.ring_body(9000, (500.0, 500.0), 300.0)
+    sc = scenes._assemble("ring", [(p, a, b)], bounds=(0.0, 0.0, 1000.0, 1000.0), sub_steps=4,
+                          link_iters=1)
+    st = sc.to_solver().plan_stats()
+    assert st["serial_bodies"] == 1
+    check(sc, 2, "large ring")
