@@ -43,6 +43,25 @@ static constexpr uint64_t kRigidSmemCap = 96 * 1024;
 static constexpr uint32_t kSerialPackBytes = 96 * 1024;  // shared memory per small-body pack
 static constexpr uint32_t kSerialPackThreads = 64;       // bodies per serial pack
 
+// Kernel launch; pdl: programmatic dependent launch — the kernel may start
+// while the previous kernel in the stream finishes (it calls pdl_wait()
+// before touching that kernel's results).
+template <typename... P, typename... A>
+static void launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     bool pdl, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1u : 0u;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 Engine::Engine(cudaStream_t stream) : stream_(stream) {
   if (!stream_) {
     cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
@@ -714,12 +733,18 @@ int Engine::launch_all(bool profiling) {
     const uint32_t sb = c.res ? c.res : 2 * c.fill;
     const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
     const uint32_t rg = c.smem ? c.region : 0u;
-    if (c.res && c.full) k_exec_groups<true, true, true><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.res) k_exec_groups<false, true, true><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.full && c.smem) k_exec_groups<true, true, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.full) k_exec_groups<true, false, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else if (c.smem) k_exec_groups<false, true, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
-    else k_exec_groups<false, false, false><<<grid, block, sm, st>>>(W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    // The sub-step pipeline's main-stream link launch follows the previous
+    // sub-step's collide kernel programmatically when its schedules are
+    // resident: at most one CTA per SM waits early, leaving the SMs the
+    // circle/polygon branch needs.  (Large streamed launches started early
+    // filled every SM and delayed that branch: 18 % slower on 1,024 bodies.)
+    const bool pdl = !profiling && !c.full && c.res && st == stream_;
+    void (*k)(const DWorld*, DScheds, const uint2*, uint32_t, uint32_t, uint32_t, uint32_t,
+              uint32_t, uint32_t, uint32_t) =
+        c.res ? (c.full ? k_exec_groups<true, true, true> : k_exec_groups<false, true, true>)
+        : c.full ? (c.smem ? k_exec_groups<true, true, false> : k_exec_groups<true, false, false>)
+                 : (c.smem ? k_exec_groups<false, true, false> : k_exec_groups<false, false, false>);
+    launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
   };
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
@@ -835,22 +860,25 @@ int Engine::launch_all(bool profiling) {
       const uint32_t subs = nsub <= 2u * (uint32_t)std::max(g_num_sms, 1) ? 1u : 4u;
       const uint32_t nt = (nsub + subs - 1) / subs;
       timed("grid_count", [&] {
-        k_grid_count<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+        launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH, nch,
+                 cur, s);
       });
       // one-sub-tile CTAs fit two per SM, four-sub-tile ones one per SM
       const uint32_t ncta =
           std::min<uint32_t>(nt, (subs == 1 ? 2u : 1u) * (uint32_t)std::max(g_num_sms, 1));
       timed("grid_scan", [&] {
-        if (subs == 1) k_grid_scan<1><<<ncta, 1024, 0, stream_>>>(grid_, grid_used_, nt);
-        else k_grid_scan<4><<<ncta, 1024, 0, stream_>>>(grid_, grid_used_, nt);
+        launch_k(subs == 1 ? k_grid_scan<1> : k_grid_scan<4>, dim3(ncta), dim3(1024), 0, stream_,
+                 !profiling, grid_, grid_used_, nt);
       });
       timed("grid_scatter", [&] {
-        k_grid_scatter<<<nch, CHUNK, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+        launch_k(k_grid_scatter, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH,
+                 nch, cur, s);
       });
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      k_collide_integrate<<<nch * COLLIDE_CTAS, COLLIDE_THREADS, 0, stream_>>>(W, grid_, CH, nch, cur, s);
+      launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0, stream_,
+               !profiling, W, grid_, CH, nch, cur, s);
     });
     if (nre) edge(stream_, ax);
   }

@@ -115,6 +115,20 @@ __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
   }
 }
 
+// Programmatic dependent launch.  The main-stream kernels of a sub-step are
+// launched so that each may start while its predecessor finishes: every CTA
+// signals early that dependents may launch, and a kernel does its work that
+// does not depend on the predecessor (schedules, link parameters) before
+// pdl_wait(), which returns once the predecessor grid has completed and its
+// memory is visible.  Every CTA calls pdl_wait() before it exits, early
+// exits included: a grid then completes only after its predecessor did, so
+// the guarantee carries down the whole chain.  Without a programmatic
+// launch both are no-ops.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ----------------------------------------------------------------------------
 // Bulk-copy (TMA) helpers.  One elected thread issues cp.async.bulk into
 // shared memory and completion is tracked by an mbarrier transaction count.
@@ -216,12 +230,19 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               uint32_t G, uint32_t region_bytes, uint32_t sched_bytes,
                               uint32_t cur, uint32_t sub) {
   extern __shared__ __align__(128) unsigned char smem[];
+  pdl_trigger();
   const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
   const uint32_t item = blockIdx.x * G + g;
-  if (item >= nlist) return;  // the whole group leaves; its barrier is private
+  if (item >= nlist) {  // the whole group leaves; its barrier is private
+    pdl_wait();
+    return;
+  }
   const uint2 wi = list[item];
   const DWorld& W = worlds[wi.x];
-  if (!FULL && sub >= W.S) return;  // world already finished its sub-steps
+  if (!FULL && sub >= W.S) {  // world already finished its sub-steps
+    pdl_wait();
+    return;
+  }
   const DBody B = W.bodies[wi.y];
   const DSched S = SC.scheds[B.sched];
   const uint32_t* bidx = W.bidx + B.i0;
@@ -274,22 +295,24 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   const uint32_t sq_a = sp_a + 8u * B.np;
   const uint32_t srs_a = sq_a + (FULL ? 8u * B.np : 0u);
   if (SMEM) {
-    // One pass issues the particle and link-parameter loads together (plain
-    // stores, so the compiler keeps many global loads in flight); a body
-    // whose particles are contiguous in the world skips the bidx indirection.
+    // Link parameters first (static during a step), then, once the
+    // previous kernel's positions are visible, the particles (plain stores,
+    // so the compiler keeps many global loads in flight); a body whose
+    // particles are contiguous in the world skips the bidx indirection.
     float2* sp = reinterpret_cast<float2*>(base);
     float2* sq = sp + B.np;
     float2* srs = sq + (FULL ? B.np : 0u);
-    const uint32_t n = B.np > B.nl ? B.np : B.nl;
 #pragma unroll 4
-    for (uint32_t i = t; i < n; i += T) {
-      if (i < B.np) {
-        const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
-        sp[i] = gp[k];
-        if (FULL) sq[i] = gq[k];
-      }
-      if (i < B.nl) srs[i] = make_float2(grest[i], gstiff[i]);
+    for (uint32_t i = t; i < B.nl; i += T) srs[i] = make_float2(grest[i], gstiff[i]);
+    pdl_wait();
+#pragma unroll 4
+    for (uint32_t i = t; i < B.np; i += T) {
+      const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
+      sp[i] = gp[k];
+      if (FULL) sq[i] = gq[k];
     }
+  } else {
+    pdl_wait();
   }
   // a resident schedule is waited for once, under the same barrier
   if (RES && t == 0 && S.nchunks > 0) flag[0] = mbar_wait_bounded(&bar[0], 0u) ? 1u : 0u;
@@ -1115,6 +1138,8 @@ constexpr uint32_t CHUNK = 320;
 static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __restrict__ worlds, DGrid G,
                                                       const uint2* __restrict__ chunks,
                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
+  pdl_trigger();
+  pdl_wait();  // positions from the link phase
   if (blockIdx.x >= nchunks) return;
   const uint2 ch = chunks[blockIdx.x];
   const DWorld& W = worlds[ch.x];
@@ -1224,6 +1249,8 @@ template <uint32_t SUBS>
 __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, uint32_t ntiles) {
   constexpr uint32_t subs = SUBS;
   __shared__ uint32_t s_tile, s_epoch, s_off;
+  pdl_trigger();
+  pdl_wait();  // counts from the count pass
   if (threadIdx.x == 0) s_epoch = *reinterpret_cast<volatile uint32_t*>(&G.tctl[2]);
   for (;;) {
     if (threadIdx.x == 0) s_tile = atomicAdd(&G.tctl[0], 1u);
@@ -1325,6 +1352,8 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
                                                         const uint2* __restrict__ chunks,
                                                         uint32_t nchunks, uint32_t cur,
                                                         uint32_t sub) {
+  pdl_trigger();
+  pdl_wait();  // ranges from the scan
   if (blockIdx.x >= nchunks) return;
   const uint2 ch = chunks[blockIdx.x];
   const DWorld& W = worlds[ch.x];
@@ -1495,6 +1524,8 @@ static_assert(COLLIDE_CTAS * (COLLIDE_THREADS / 32) * COLLIDE_PER_WARP == CHUNK,
 static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate(
     const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
+  pdl_trigger();
+  pdl_wait();  // sorted entries from the scatter (and everything before it)
   const uint32_t cidx = blockIdx.x / COLLIDE_CTAS;
   if (cidx >= nchunks) return;
   const uint2 ch = chunks[cidx];
