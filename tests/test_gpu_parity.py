@@ -468,3 +468,17 @@ def test_ring_too_large_for_shared_memory_runs_serially_from_global(gpu):
     st = sc.to_solver().plan_stats()
     assert st["serial_bodies"] == 1
     check(sc, 2, "large ring")
+
+
+def test_programmatic_launches_do_not_change_results(gpu):
+    """The sub-step pipeline's kernels start early under programmatic
+    dependent launch; profiling mode launches them one after another
+    without it.  Both give the same bits."""
+    from bendy2d_gb300 import scenes
+    sc = scenes.config2(seed=14, n_bodies=5, box=120.0, n_circles=3, n_polys=2)
+    a, b = sc.to_solver(), sc.to_solver()
+    b.set_profiling(True)
+    for _ in range(4):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    assert_same_state(solver_state(a), solver_state(b), "programmatic vs serial launches")
