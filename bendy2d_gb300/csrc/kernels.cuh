@@ -1139,13 +1139,15 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
                                                       const uint2* __restrict__ chunks,
                                                       uint32_t nchunks, uint32_t cur, uint32_t sub) {
   pdl_trigger();
-  pdl_wait();  // positions from the link phase
-  if (blockIdx.x >= nchunks) return;
-  const uint2 ch = chunks[blockIdx.x];
+  // chunk and world records are fixed during a step: read before the wait
+  const uint2 ch = chunks[blockIdx.x < nchunks ? blockIdx.x : 0u];
   const DWorld& W = worlds[ch.x];
   const uint32_t j = ch.y + threadIdx.x;
-  if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
-  const float2 p = W.pos[cur][j];
+  const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S && (W.flags & COLLIDE_PP);
+  const float2* P = W.pos[cur];
+  pdl_wait();  // positions from the link phase
+  if (!act) return;
+  const float2 p = P[j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
   const uint32_t b = bucket_of(W, cx, cy);
   const uint32_t r = atomicAdd(&G.count[b], 1u);
@@ -1353,13 +1355,15 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
                                                         uint32_t nchunks, uint32_t cur,
                                                         uint32_t sub) {
   pdl_trigger();
-  pdl_wait();  // ranges from the scan
-  if (blockIdx.x >= nchunks) return;
-  const uint2 ch = chunks[blockIdx.x];
+  // chunk and world records are fixed during a step: read before the wait
+  const uint2 ch = chunks[blockIdx.x < nchunks ? blockIdx.x : 0u];
   const DWorld& W = worlds[ch.x];
   const uint32_t j = ch.y + threadIdx.x;
-  if (j >= W.np || sub >= W.S || !(W.flags & COLLIDE_PP)) return;
-  const float2 p = W.pos[cur][j];
+  const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S && (W.flags & COLLIDE_PP);
+  const float2* P = W.pos[cur];
+  pdl_wait();  // ranges from the scan
+  if (!act) return;
+  const float2 p = P[j];
   const uint2 br = G.pbr[W.gp0 + j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
   G.sorted[G.range[br.x].x + br.y] =
@@ -1525,12 +1529,12 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
     const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
   pdl_trigger();
-  pdl_wait();  // sorted entries from the scatter (and everything before it)
+  // chunk and world records are fixed during a step: read before the wait
   const uint32_t cidx = blockIdx.x / COLLIDE_CTAS;
-  if (cidx >= nchunks) return;
-  const uint2 ch = chunks[cidx];
+  const uint2 ch = chunks[cidx < nchunks ? cidx : 0u];
   const DWorld& W = worlds[ch.x];
-  if (sub >= W.S) return;  // uniform over the CTA
+  pdl_wait();  // sorted entries from the scatter (and everything before it)
+  if (cidx >= nchunks || sub >= W.S) return;  // uniform over the CTA
   const uint32_t wl = threadIdx.x & 31u, grp = wl / 3u, row = wl - 3u * grp;
   const uint32_t i = ch.y + (blockIdx.x % COLLIDE_CTAS) * (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP) +
                      (threadIdx.x >> 5) * COLLIDE_PER_WARP + grp;
