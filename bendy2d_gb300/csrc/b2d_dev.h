@@ -127,7 +127,7 @@ struct DScheds {
   const uint32_t* stream;
   uint32_t* err;
 };
-enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_SCAN_TIMEOUT = 2u };
+enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_GRID_OVERFLOW = 2u };
 
 // Extension broadphase: hashed uniform grid built by a counting sort each
 // sub-step.  Every world with particle collisions owns a power-of-two range
@@ -136,14 +136,13 @@ constexpr uint32_t SCAN_SUB = 4096;  // buckets per scan sub-tile (1024 threads 
                                      // tile is 1 or 4 sub-tiles
 struct DGrid {
   uint32_t* count;       // nbuckets: entries per bucket (all zero between sub-steps)
-  uint2* range;          // nbuckets: {exclusive prefix sum of count, count}
-  unsigned long long* tstate;  // per scan tile: {epoch << 2 | kind, value}, kind 1 = tile
-                               // sum, 2 = inclusive prefix (decoupled look-back)
-  uint32_t* tctl;        // scan control: [0] next tile id, [1] tiles done, [2] epoch
+  uint2* range;          // nbuckets: {first entry in sorted, count}
+  uint32_t* cursor;      // entries of sorted handed out so far this sub-step
   uint2* pbr;            // per particle: (bucket, rank within bucket)
-  uint4* sorted;         // per particle: {pos.x bits, pos.y bits, cell x, cell y}
+  uint4* sorted;         // cap entries: {pos.x bits, pos.y bits, cell x, cell y}
   uint32_t* err;         // device error word (ERR_BIT_*)
   uint32_t nbuckets;
+  uint32_t cap;
 };
 
 }  // namespace b2d

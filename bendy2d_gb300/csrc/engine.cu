@@ -346,7 +346,8 @@ int Engine::check_device_error() {
     grid_reset_ = true;
     B2D_CUDA(cudaMemsetAsync(d_err_, 0, 4, stream_));
     last_error = "device error word " + std::to_string(e) +
-                 ((e & ERR_BIT_TMA_TIMEOUT) ? " (a bulk-copy wait timed out)" : "");
+                 ((e & ERR_BIT_TMA_TIMEOUT) ? " (a bulk-copy wait timed out)" : "") +
+                 ((e & ERR_BIT_GRID_OVERFLOW) ? " (grid entries past their capacity)" : "");
     return ERR_DEVICE;
   }
   return OK;
@@ -356,11 +357,10 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   if (nbuckets <= grid_.nbuckets && np_pp <= grid_np_ && d_grid_) return OK;
   const size_t nb = std::max(nbuckets, (size_t)grid_.nbuckets);
   const size_t np = std::max<size_t>(std::max(np_pp, grid_np_), 1);
-  const size_t ntiles = (nb + SCAN_SUB - 1) / SCAN_SUB;  // most tiles: one sub-tile each
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
-  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_tstate = seg(ntiles * 8),
-               o_tctl = seg(16), o_pbr = seg(np * 8), o_sorted = seg(np * 16);
+  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_cursor = seg(4),
+               o_pbr = seg(np * 8), o_sorted = seg(np * 16);
   B2D_CUDA(cudaStreamSynchronize(stream_));
   if (d_grid_) dev_bytes_ -= grid_bytes_;
   cudaFree(d_grid_);
@@ -369,11 +369,11 @@ int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
   B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
   grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
   grid_.range = reinterpret_cast<uint2*>(d_grid_ + o_start);
-  grid_.tstate = reinterpret_cast<unsigned long long*>(d_grid_ + o_tstate);
-  grid_.tctl = reinterpret_cast<uint32_t*>(d_grid_ + o_tctl);
+  grid_.cursor = reinterpret_cast<uint32_t*>(d_grid_ + o_cursor);
   grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o_pbr);
   grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o_sorted);
   grid_.nbuckets = (uint32_t)nb;
+  grid_.cap = (uint32_t)np;
   grid_np_ = np;
   grid_bytes_ = bytes;
   grid_head_bytes_ = o_pbr;
@@ -854,8 +854,8 @@ int Engine::launch_all(bool profiling) {
     }
     end_pass();
     if (any_pp_) {
-      // counts are all zero here: the scan of the previous sub-step cleared them
-      // tiles of one sub-tile while that gives at most two per SM, else four
+      // counts are all zero here: the scan of the previous sub-step cleared them.
+      // Tiles of one sub-tile while that gives at most two per SM, else four.
       const uint32_t nsub = (grid_used_ + SCAN_SUB - 1) / SCAN_SUB;
       const uint32_t subs = nsub <= 2u * (uint32_t)std::max(g_num_sms, 1) ? 1u : 4u;
       const uint32_t nt = (nsub + subs - 1) / subs;
@@ -901,7 +901,7 @@ int Engine::step() {
   if (lists_dirty_ && (st = rebuild_lists()) != OK) return st;
   if ((st = upload_registry()) != OK) return st;
   if (grid_reset_ && d_grid_) {
-    // after a failed step the bucket counts and scan words may be partial
+    // after a failed step the bucket counts and the cursor may be partial
     B2D_CUDA(cudaMemsetAsync(d_grid_, 0, grid_head_bytes_, stream_));
     grid_reset_ = false;
   }

@@ -1146,67 +1146,14 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S && (W.flags & COLLIDE_PP);
   const float2* P = W.pos[cur];
   pdl_wait();  // positions from the link phase
+  // the previous sub-step's scatter and collide are done with the cursor
+  if (blockIdx.x == 0 && threadIdx.x == 0) *G.cursor = 0u;
   if (!act) return;
   const float2 p = P[j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
   const uint32_t b = bucket_of(W, cx, cy);
   const uint32_t r = atomicAdd(&G.count[b], 1u);
   G.pbr[W.gp0 + j] = make_uint2(b, r);
-}
-
-// block-wide exclusive scan of one value per thread (blockDim = 1024)
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
-  __shared__ uint32_t warp_sum[32];
-  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-    if (lane >= (uint32_t)o) x += y;
-  }
-  if (lane == 31) warp_sum[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    const uint32_t nw = blockDim.x >> 5;
-    uint32_t w = lane < nw ? warp_sum[lane] : 0u;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-      if (lane >= (uint32_t)o) w += y;
-    }
-    warp_sum[lane] = w;  // inclusive
-  }
-  __syncthreads();
-  const uint32_t before = wid ? warp_sum[wid - 1] : 0u;
-  if (total) *total = warp_sum[(blockDim.x >> 5) - 1];
-  __syncthreads();
-  return before + x - v;
-}
-
-// Single-pass exclusive scan of the bucket counts into ranges, by decoupled
-// look-back (D. Merrill, M. Garland, "Single-pass Parallel Prefix Scan with
-// Decoupled Look-back", NVIDIA tech report NVR-2016-002).  Persistent CTAs
-// take tile ids in order from a counter; each tile publishes its sum, then
-// walks back over its predecessors' published words (sums, or inclusive
-// prefixes, which end the walk) and publishes its own inclusive prefix.  A
-// tile only waits on tiles with smaller ids, which running CTAs had already
-// taken and publish without waiting, so the walk always ends; it is bounded
-// all the same and records ERR_BIT_SCAN_TIMEOUT if it gives up.  Published
-// words carry a launch epoch, so no clearing is needed between launches; the
-// last CTA to finish resets the counters and advances the epoch.  The scan
-// also zeroes the counts it read, leaving them ready for the next sub-step's
-// count pass.
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long scan_word(uint32_t epoch, uint32_t kind,
-                                                        uint32_t value) {
-  return ((unsigned long long)((epoch << 2) | kind) << 32) | value;
 }
 
 // block-wide exclusive scan of four values per thread at once (blockDim =
@@ -1242,32 +1189,37 @@ __device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
                     before.w + x.w - v.w);
 }
 
-// Persistent: each CTA takes tiles (SUBS sub-tiles of SCAN_SUB buckets,
-// SUBS = 1 or 4: small grids favour more tiles, large ones fewer) in id
-// order until none is left.  Within a tile, thread t holds buckets
-// sub * SCAN_SUB + 4t .. +3 of each sub-tile, so every load and store of a
-// warp is contiguous.
+// Bucket ranges from the counts.  Each tile (SUBS sub-tiles of SCAN_SUB
+// buckets; SUBS = 1 or 4: small grids favour more tiles, large ones fewer)
+// scans its counts and takes one block of `sorted`, of the tile's total size,
+// from the sub-step's cursor with a single atomic.  Tiles do not wait on one
+// another: a bucket's entries stay contiguous and the buckets of a tile stay
+// in order (neighbouring cells' buckets are neighbours, which keeps the
+// collide pass's loads together), but the tiles land in `sorted` in the order
+// their atomics ran.  Nothing reads that order: the contact sums are exact
+// integer sums, so the order of a bucket's entries does not matter either
+// (it already follows the count pass's atomics).  The count pass reset the
+// cursor; a block that would end past `cap` (a cursor left over from a failed
+// launch) is not handed out: its buckets get empty ranges and
+// ERR_BIT_GRID_OVERFLOW is set.  The scan also zeroes the counts it read,
+// leaving them ready for the next sub-step's count pass.  Within a tile,
+// thread t holds buckets sub * SCAN_SUB + 4t .. +3 of each sub-tile, so every
+// load and store of a warp is contiguous.
 template <uint32_t SUBS>
 __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, uint32_t ntiles) {
-  constexpr uint32_t subs = SUBS;
-  __shared__ uint32_t s_tile, s_epoch, s_off;
+  __shared__ uint32_t s_base, s_ok;
   pdl_trigger();
-  pdl_wait();  // counts from the count pass
-  if (threadIdx.x == 0) s_epoch = *reinterpret_cast<volatile uint32_t*>(&G.tctl[2]);
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(&G.tctl[0], 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile, ep = s_epoch & 0x3FFFFFFFu;
-    if (tile >= ntiles) break;  // uniform
+  pdl_wait();  // counts and the cursor reset from the count pass
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     // bucket ranges are whole multiples of 64, so each group of four counts
     // is either all inside or all outside
     uint4 c[4];
     uint4 v = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
-      const uint32_t base = (tile * subs + k) * SCAN_SUB + threadIdx.x * 4u;
+      const uint32_t base = (tile * SUBS + k) * SCAN_SUB + threadIdx.x * 4u;
       c[k] = make_uint4(0u, 0u, 0u, 0u);
-      if (k < subs && base < nbuckets) {
+      if (k < SUBS && base < nbuckets) {
         uint4* cp = reinterpret_cast<uint4*>(G.count + base);
         c[k] = *cp;
         *cp = make_uint4(0u, 0u, 0u, 0u);  // ready for the next count pass
@@ -1279,74 +1231,32 @@ __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, 
     v.w = c[3].x + c[3].y + c[3].z + c[3].w;
     uint4 sub_tot;
     const uint4 excl = block_exclusive_scan4(v, &sub_tot);
-    const uint32_t tot = sub_tot.x + sub_tot.y + sub_tot.z + sub_tot.w;
-    if (threadIdx.x == 0)
-      st_release_u64(&G.tstate[tile], scan_word(ep, tile == 0 ? 2u : 1u, tot));
-    if (threadIdx.x < 32u) {
-      // warp 0 looks back over windows of 32 predecessors: lane i reads tile
-      // (end - 1 - i); the window sums up to the nearest inclusive prefix
-      const uint32_t lane = threadIdx.x;
-      uint32_t off = 0;
-      int end = (int)tile;
-      const long long deadline = clock64() + WAIT_LIMIT_CYCLES;
-      bool timed_out = false;
-      while (end > 0) {
-        const int p = end - 1 - (int)lane;
-        unsigned long long w = scan_word(ep, 2u, 0u);  // before tile 0: prefix 0
-        uint32_t kind = 2u;
-        for (;;) {
-          if (p >= 0) {
-            w = ld_acquire_u64(&G.tstate[p]);
-            const uint32_t hi = (uint32_t)(w >> 32);
-            kind = (hi >> 2) == ep ? (hi & 3u) : 0u;
-          }
-          if (__all_sync(0xFFFFFFFFu, kind != 0u)) break;
-          if (__any_sync(0xFFFFFFFFu, clock64() > deadline)) {  // warp-uniform
-            timed_out = true;
-            break;
-          }
-        }
-        if (timed_out) break;
-        const uint32_t inc = __ballot_sync(0xFFFFFFFFu, kind == 2u);
-        const uint32_t stop = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;  // nearest prefix
-        uint32_t s = lane <= stop ? (uint32_t)w : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
-        off += s;
-        if (inc) break;
-        end -= 32;
-      }
-      if (lane == 0) {
-        if (timed_out) atomicOr(G.err, ERR_BIT_SCAN_TIMEOUT);
-        if (tile != 0) st_release_u64(&G.tstate[tile], scan_word(ep, 2u, off + tot));
-        s_off = off;
-      }
+    if (threadIdx.x == 0) {
+      const uint32_t tot = sub_tot.x + sub_tot.y + sub_tot.z + sub_tot.w;
+      const uint32_t at = tot ? atomicAdd(G.cursor, tot) : 0u;
+      const bool ok = at <= G.cap && tot <= G.cap - at;
+      if (!ok) atomicOr(G.err, ERR_BIT_GRID_OVERFLOW);
+      s_base = at;
+      s_ok = ok ? 1u : 0u;
     }
     __syncthreads();
+    const uint32_t ok = s_ok;
     const uint32_t sub_off[4] = {0u, sub_tot.x, sub_tot.x + sub_tot.y,
                                  sub_tot.x + sub_tot.y + sub_tot.z};
     const uint32_t ex[4] = {excl.x, excl.y, excl.z, excl.w};
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
-      const uint32_t base = (tile * subs + k) * SCAN_SUB + threadIdx.x * 4u;
-      if (k < subs && base < nbuckets) {
-        uint32_t run = s_off + sub_off[k] + ex[k];
+      const uint32_t base = (tile * SUBS + k) * SCAN_SUB + threadIdx.x * 4u;
+      if (k < SUBS && base < nbuckets) {
+        uint32_t run = s_base + sub_off[k] + ex[k];
+        const uint4 n = ok ? c[k] : make_uint4(0u, 0u, 0u, 0u);
         uint4* rp = reinterpret_cast<uint4*>(G.range + base);  // two {start, count} pairs each
-        rp[0] = make_uint4(run, c[k].x, run + c[k].x, c[k].y);
-        run += c[k].x + c[k].y;
-        rp[1] = make_uint4(run, c[k].z, run + c[k].z, c[k].w);
+        rp[0] = make_uint4(run, n.x, run + n.x, n.y);
+        run += n.x + n.y;
+        rp[1] = make_uint4(run, n.z, run + n.z, n.w);
       }
     }
-    __syncthreads();  // s_tile and s_off are rewritten by the next tile
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(&G.tctl[1], 1u) == gridDim.x - 1u) {  // last CTA: reset for the next launch
-      G.tctl[0] = 0u;
-      G.tctl[1] = 0u;
-      G.tctl[2] = (s_epoch + 1u) & 0x3FFFFFFFu;
-      __threadfence();
-    }
+    __syncthreads();  // s_base and s_ok are rewritten by the next tile
   }
 }
 
@@ -1365,8 +1275,10 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
   if (!act) return;
   const float2 p = P[j];
   const uint2 br = G.pbr[W.gp0 + j];
+  const uint2 rg = G.range[br.x];
+  if (br.y >= rg.y) return;  // the bucket's block was not handed out (ERR_BIT_GRID_OVERFLOW)
   const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
-  G.sorted[G.range[br.x].x + br.y] =
+  G.sorted[rg.x + br.y] =
       make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), (uint32_t)cx, (uint32_t)cy);
 }
 

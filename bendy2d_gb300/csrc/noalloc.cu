@@ -12,11 +12,11 @@
 // that loads the library until the process exits.  Every call shares it and
 // it keeps the previous call's contents, so each call clears what must start
 // at zero; calls whose GPU work overlaps (different streams, or host threads
-// racing) corrupt each other.  The bucket scan's control words also live
-// there and maintain themselves across calls (launch epochs); its bounded
-// wait records ERR_BIT_SCAN_TIMEOUT in a scratch word (O_ERR) that a
-// debugger can read, since this asynchronous call returns before the GPU
-// work runs.
+// racing) corrupt each other.  The scan's cursor lives there too (the count
+// pass resets it every sub-step); a range past the scratch entries would be
+// refused and recorded as ERR_BIT_GRID_OVERFLOW in a scratch word (O_ERR)
+// that a debugger can read, since this asynchronous call returns before the
+// GPU work runs.
 //
 // First call on a device: it resolves the array's device address with
 // cudaGetSymbolAddress while that device is current.  Make that first call
@@ -39,7 +39,6 @@ namespace {
 constexpr uint32_t NOALLOC_MAX_PARTICLES = 65536;
 constexpr uint32_t NOALLOC_MAX_BUCKETS = 2 * NOALLOC_MAX_PARTICLES;  // power of two >= 2n
 constexpr uint32_t NOALLOC_MAX_CHUNKS = (NOALLOC_MAX_PARTICLES + CHUNK - 1) / CHUNK;
-constexpr uint32_t NOALLOC_MAX_TILES = (NOALLOC_MAX_BUCKETS + SCAN_SUB - 1) / SCAN_SUB;
 
 constexpr size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 // layout of the scratch array
@@ -47,9 +46,8 @@ constexpr size_t O_WORLD = 0;
 constexpr size_t O_CHUNKS = O_WORLD + up256(sizeof(DWorld));
 constexpr size_t O_COUNT = O_CHUNKS + up256(8 * NOALLOC_MAX_CHUNKS);
 constexpr size_t O_RANGE = O_COUNT + up256(4 * NOALLOC_MAX_BUCKETS);
-constexpr size_t O_TSTATE = O_RANGE + up256(8 * NOALLOC_MAX_BUCKETS);
-constexpr size_t O_TCTL = O_TSTATE + up256(8 * NOALLOC_MAX_TILES);
-constexpr size_t O_ERR = O_TCTL + 256;
+constexpr size_t O_CURSOR = O_RANGE + up256(8 * NOALLOC_MAX_BUCKETS);
+constexpr size_t O_ERR = O_CURSOR + 256;
 constexpr size_t O_PBR = O_ERR + 256;
 constexpr size_t O_SORTED = O_PBR + up256(8 * NOALLOC_MAX_PARTICLES);
 constexpr size_t O_POS1 = O_SORTED + up256(16 * NOALLOC_MAX_PARTICLES);
@@ -142,12 +140,12 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   DGrid G;
   G.count = reinterpret_cast<uint32_t*>(base + O_COUNT);
   G.range = reinterpret_cast<uint2*>(base + O_RANGE);
-  G.tstate = reinterpret_cast<unsigned long long*>(base + O_TSTATE);
-  G.tctl = reinterpret_cast<uint32_t*>(base + O_TCTL);
+  G.cursor = reinterpret_cast<uint32_t*>(base + O_CURSOR);
   G.err = reinterpret_cast<uint32_t*>(base + O_ERR);
   G.pbr = reinterpret_cast<uint2*>(base + O_PBR);
   G.sorted = reinterpret_cast<uint4*>(base + O_SORTED);
   G.nbuckets = nb;
+  G.cap = np;
 
   k_noalloc_setup<<<(nch + 255) / 256, 256, 0, st>>>(w, chunks, nch, dW);
   // bucket counts start from zero (each scan clears what it read; this also
