@@ -1286,22 +1286,56 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_scatter(const DWorld* __r
 // round to nearest even), which makes the sum independent of the order in
 // which neighbours are found.
 __device__ __forceinline__ long long fix32(float c) { return __float2ll_rn(fmul(c, 4294967296.0f)); }
+// A contact sum converts back as float(double(s) * 2^-32).
+// For |s| < 2^53 the double holds s exactly, so that is one rounding of
+// s * 2^-32 to float, which equals rounding s to float and scaling by 2^-32
+// (exact: every nonzero result is a normal float between 2^-32 and 2^21).
+// That form needs no FP64 instruction; larger sums take the double path.
 __device__ __forceinline__ float unfix32(long long s) {
+  if (s > -(1LL << 53) && s < (1LL << 53)) return fmul(__ll2float_rn(s), 2.3283064365386962890625e-10f);
   return __double2float_rn(__dmul_rn(__ll2double_rn(s), 2.3283064365386962890625e-10));
 }
 
-__device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D2, long long& sx,
-                                           long long& sy, bool& hit) {
+// Contacts found by one lane's neighbour walk.  The IEEE square root and
+// divisions of a contact (the costly part) are not run inside the walk, where
+// a warp would pay for them on every step in which any of its lanes meets a
+// contact, but after it: the first CONTACT_SLOTS contacts of a lane wait in
+// registers and are solved together at the end (further ones are solved on
+// the spot).  The sums are integers, so the order of the solves cannot
+// change them.
+constexpr uint32_t CONTACT_SLOTS = 2;
+struct Contacts {
+  float dx[CONTACT_SLOTS], dy[CONTACT_SLOTS], d2[CONTACT_SLOTS];
+  uint32_t n;
+  long long sx, sy;
+  bool hit;
+};
+__device__ __forceinline__ void contact_solve(float dx, float dy, float d2, float D, Contacts& c) {
+  const float dist = fsqrt(d2);
+  const float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
+  const float ov = fsub(D, dist);
+  c.sx += fix32(fmul(fmul(nx, ov), 0.5f));
+  c.sy += fix32(fmul(fmul(ny, ov), 0.5f));
+  c.hit = true;
+}
+__device__ __forceinline__ void pp_contact(float2 p, float2 pj, float D, float D2, Contacts& c) {
   const float dx = fsub(p.x, pj.x), dy = fsub(p.y, pj.y);
   const float d2 = fadd(fmul(dx, dx), fmul(dy, dy));
   if (d2 < D2 && d2 > 0.0f) {
-    const float dist = fsqrt(d2);
-    const float nx = fdiv(dx, dist), ny = fdiv(dy, dist);
-    const float ov = fsub(D, dist);
-    sx += fix32(fmul(fmul(nx, ov), 0.5f));
-    sy += fix32(fmul(fmul(ny, ov), 0.5f));
-    hit = true;
+    if (c.n < CONTACT_SLOTS) {
+#pragma unroll
+      for (uint32_t k = 0; k < CONTACT_SLOTS; ++k)
+        if (k == c.n) { c.dx[k] = dx; c.dy[k] = dy; c.d2[k] = d2; }
+      ++c.n;
+    } else {
+      contact_solve(dx, dy, d2, D, c);
+    }
   }
+}
+__device__ __forceinline__ void contacts_finish(float D, Contacts& c) {
+#pragma unroll
+  for (uint32_t k = 0; k < CONTACT_SLOTS; ++k)
+    if (k < c.n) contact_solve(c.dx[k], c.dy[k], c.d2[k], D, c);
 }
 
 // particle-Circle (circles are kinematic for particles; index order)
@@ -1377,11 +1411,11 @@ static __device__ float2 particle_polygon(const DWorld& W, uint32_t k, float2 p)
 // d2 = 0, which pp_contact never counts as a contact.
 __device__ __forceinline__ void visit_cell(const DGrid& G, float2 p, int32_t ncx, int32_t ncy,
                                            uint32_t s0, uint32_t cnt, float D, float D2,
-                                           long long& sx, long long& sy, bool& hit) {
+                                           Contacts& c) {
   for (uint32_t k = s0; k < s0 + cnt; ++k) {
     const uint4 e = G.sorted[k];
     if (e.z != (uint32_t)ncx || e.w != (uint32_t)ncy) continue;
-    pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, sx, sy, hit);
+    pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, c);
   }
 }
 
@@ -1456,8 +1490,11 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
   float2 p = act ? P[i] : make_float2(0.f, 0.f);
   float2 q = own ? W.prev[i] : make_float2(0.f, 0.f);  // issued early, used last
   if (W.flags & COLLIDE_PP) {  // uniform over the CTA
-    long long sx = 0, sy = 0;
-    bool hit = false;
+    Contacts c;
+    c.n = 0;
+    c.sx = 0;
+    c.sy = 0;
+    c.hit = false;
     if (act) {
       const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell);
       const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell) + (int32_t)row - 1;  // this lane's row
@@ -1466,10 +1503,13 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
       const uint32_t b0 = bucket_of(W, cx - 1, cy), b1 = bucket_of(W, cx, cy),
                      b2 = bucket_of(W, cx + 1, cy);
       const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2];
-      visit_cell(G, p, cx - 1, cy, r0.x, r0.y, D, D2, sx, sy, hit);
-      visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, sx, sy, hit);
-      visit_cell(G, p, cx + 1, cy, r2.x, r2.y, D, D2, sx, sy, hit);
+      visit_cell(G, p, cx - 1, cy, r0.x, r0.y, D, D2, c);
+      visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, c);
+      visit_cell(G, p, cx + 1, cy, r2.x, r2.y, D, D2, c);
+      contacts_finish(D, c);
     }
+    long long sx = c.sx, sy = c.sy;
+    bool hit = c.hit;
     // the owner adds the other two rows' sums (lanes 30, 31 read lanes 31, 0:
     // harmless, they own nothing)
     const uint32_t l1 = (wl + 1u) & 31u, l2 = (wl + 2u) & 31u;

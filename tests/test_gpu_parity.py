@@ -190,6 +190,20 @@ def test_heavy_polygon_and_circle_contacts(gpu):
     check(sc, 12, "pile")
 
 
+def test_contact_sums_past_2_pow_53(gpu):
+    """Particles millions of units wide, all overlapping: a particle's
+    fixed-point contact sum passes 2^53, where it converts back through the
+    double path; smaller sums take the float path."""
+    from bendy2d_gb300 import scenes
+    from bendy2d_gb300.scenes import COLLIDE_PP
+    rng = np.random.default_rng(13)
+    pos = (rng.uniform(4.0e8, 4.02e8, size=(24, 2))).astype(np.float32)
+    free = (pos, np.zeros(0, np.uint64), np.zeros(0, np.uint64))
+    sc = scenes._assemble("wide", [free], bounds=(0.0, 0.0, 1.0e9, 1.0e9), sub_steps=2,
+                          link_iters=1, collide=COLLIDE_PP, radius=3.0e6, cell=8388608.0)
+    check(sc, 3, "wide contacts")
+
+
 def test_circle_links_and_static_circles(gpu):
     from bendy2d_gb300 import scenes
     rng = np.random.default_rng(4)
