@@ -132,8 +132,11 @@ enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_GRID_OVERFLOW = 2u };
 // Extension broadphase: hashed uniform grid built by a counting sort each
 // sub-step.  Every world with particle collisions owns a power-of-two range
 // of buckets; a bucket's entries are contiguous in `sorted`.
-constexpr uint32_t SCAN_SUB = 4096;  // buckets per scan sub-tile (1024 threads x 4); a
-                                     // tile is 1 or 4 sub-tiles
+// bucket scan tiles: 1,024 buckets (256 threads x 4 each) for grids of up to
+// SCAN_SMALL_MAX buckets, else 16,384 (four sub-tiles of 1024 threads x 4)
+constexpr uint32_t SCAN_SMALL_TILE = 1024;
+constexpr uint32_t SCAN_LARGE_TILE = 16384;
+constexpr uint32_t SCAN_SMALL_MAX = 1u << 20;
 struct DGrid {
   uint32_t* count;       // nbuckets: entries per bucket (all zero between sub-steps)
   uint2* range;          // nbuckets: {first entry in sorted, count}

@@ -855,20 +855,23 @@ int Engine::launch_all(bool profiling) {
     end_pass();
     if (any_pp_) {
       // counts are all zero here: the scan of the previous sub-step cleared them.
-      // Tiles of one sub-tile while that gives at most two per SM, else four.
-      const uint32_t nsub = (grid_used_ + SCAN_SUB - 1) / SCAN_SUB;
-      const uint32_t subs = nsub <= 2u * (uint32_t)std::max(g_num_sms, 1) ? 1u : 4u;
-      const uint32_t nt = (nsub + subs - 1) / subs;
+      // Small grids: one 256-thread CTA per 1,024-bucket tile; large ones:
+      // 16,384-bucket tiles over at most one 1024-thread CTA per SM.
+      const bool small = grid_used_ <= SCAN_SMALL_MAX;
+      const uint32_t tile = small ? SCAN_SMALL_TILE : SCAN_LARGE_TILE;
+      const uint32_t nt = (grid_used_ + tile - 1) / tile;
       timed("grid_count", [&] {
         launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH, nch,
                  cur, s);
       });
-      // one-sub-tile CTAs fit two per SM, four-sub-tile ones one per SM
-      const uint32_t ncta =
-          std::min<uint32_t>(nt, (subs == 1 ? 2u : 1u) * (uint32_t)std::max(g_num_sms, 1));
+      const uint32_t ncta = small ? nt : std::min<uint32_t>(nt, (uint32_t)std::max(g_num_sms, 1));
       timed("grid_scan", [&] {
-        launch_k(subs == 1 ? k_grid_scan<1> : k_grid_scan<4>, dim3(ncta), dim3(1024), 0, stream_,
-                 !profiling, grid_, grid_used_, nt);
+        if (small)
+          launch_k(k_grid_scan<1, 256>, dim3(ncta), dim3(256), 0, stream_, !profiling, grid_,
+                   grid_used_, nt);
+        else
+          launch_k(k_grid_scan<4, 1024>, dim3(ncta), dim3(1024), 0, stream_, !profiling, grid_,
+                   grid_used_, nt);
       });
       timed("grid_scatter", [&] {
         launch_k(k_grid_scatter, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH,

@@ -1156,11 +1156,14 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   G.pbr[W.gp0 + j] = make_uint2(b, r);
 }
 
-// block-wide exclusive scan of four values per thread at once (blockDim =
-// 1024); the four lanes scan independently.  Returns the exclusive prefix of
-// each lane and stores the four block totals in *total.
+// block-wide exclusive scan of four values per thread at once (THREADS a
+// multiple of 32, at most 1024); the four lanes scan independently.
+// Returns the exclusive prefix of each lane and stores the four block
+// totals in *total.
+template <uint32_t THREADS>
 __device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
-  __shared__ uint4 warp_sum4[32];
+  constexpr uint32_t NW = THREADS / 32;
+  __shared__ uint4 warp_sum4[NW];
   const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
   uint4 x = v;
 #pragma unroll
@@ -1172,25 +1175,25 @@ __device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
   if (lane == 31) warp_sum4[wid] = x;
   __syncthreads();
   if (wid == 0) {
-    uint4 w = warp_sum4[lane];  // blockDim is 1024: 32 warps
+    uint4 w = lane < NW ? warp_sum4[lane] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < (int)NW; o <<= 1) {
       const uint32_t y0 = __shfl_up_sync(0xFFFFFFFFu, w.x, o), y1 = __shfl_up_sync(0xFFFFFFFFu, w.y, o),
                      y2 = __shfl_up_sync(0xFFFFFFFFu, w.z, o), y3 = __shfl_up_sync(0xFFFFFFFFu, w.w, o);
       if (lane >= (uint32_t)o) { w.x += y0; w.y += y1; w.z += y2; w.w += y3; }
     }
-    warp_sum4[lane] = w;  // inclusive
+    if (lane < NW) warp_sum4[lane] = w;  // inclusive
   }
   __syncthreads();
   const uint4 before = wid ? warp_sum4[wid - 1] : make_uint4(0u, 0u, 0u, 0u);
-  *total = warp_sum4[31];
+  *total = warp_sum4[NW - 1];
   __syncthreads();
   return make_uint4(before.x + x.x - v.x, before.y + x.y - v.y, before.z + x.z - v.z,
                     before.w + x.w - v.w);
 }
 
-// Bucket ranges from the counts.  Each tile (SUBS sub-tiles of SCAN_SUB
-// buckets; SUBS = 1 or 4: small grids favour more tiles, large ones fewer)
+// Bucket ranges from the counts.  Each tile (SUBS sub-tiles of 4 x THREADS
+// buckets: small grids favour many small tiles, large ones fewer)
 // scans its counts and takes one block of `sorted`, of the tile's total size,
 // from the sub-step's cursor with a single atomic.  Tiles do not wait on one
 // another: a bucket's entries stay contiguous and the buckets of a tile stay
@@ -1203,10 +1206,11 @@ __device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
 // launch) is not handed out: its buckets get empty ranges and
 // ERR_BIT_GRID_OVERFLOW is set.  The scan also zeroes the counts it read,
 // leaving them ready for the next sub-step's count pass.  Within a tile,
-// thread t holds buckets sub * SCAN_SUB + 4t .. +3 of each sub-tile, so every
-// load and store of a warp is contiguous.
-template <uint32_t SUBS>
-__global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, uint32_t ntiles) {
+// thread t holds buckets 4t .. 4t+3 of each sub-tile, so every load and
+// store of a warp is contiguous.
+template <uint32_t SUBS, uint32_t THREADS>
+__global__ void __launch_bounds__(THREADS) k_grid_scan(DGrid G, uint32_t nbuckets, uint32_t ntiles) {
+  constexpr uint32_t SUB = 4u * THREADS;
   __shared__ uint32_t s_base, s_ok;
   pdl_trigger();
   pdl_wait();  // counts and the cursor reset from the count pass
@@ -1217,7 +1221,7 @@ __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, 
     uint4 v = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
-      const uint32_t base = (tile * SUBS + k) * SCAN_SUB + threadIdx.x * 4u;
+      const uint32_t base = (tile * SUBS + k) * SUB + threadIdx.x * 4u;
       c[k] = make_uint4(0u, 0u, 0u, 0u);
       if (k < SUBS && base < nbuckets) {
         uint4* cp = reinterpret_cast<uint4*>(G.count + base);
@@ -1230,7 +1234,7 @@ __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, 
     v.z = c[2].x + c[2].y + c[2].z + c[2].w;
     v.w = c[3].x + c[3].y + c[3].z + c[3].w;
     uint4 sub_tot;
-    const uint4 excl = block_exclusive_scan4(v, &sub_tot);
+    const uint4 excl = block_exclusive_scan4<THREADS>(v, &sub_tot);
     if (threadIdx.x == 0) {
       const uint32_t tot = sub_tot.x + sub_tot.y + sub_tot.z + sub_tot.w;
       const uint32_t at = tot ? atomicAdd(G.cursor, tot) : 0u;
@@ -1246,7 +1250,7 @@ __global__ void __launch_bounds__(1024) k_grid_scan(DGrid G, uint32_t nbuckets, 
     const uint32_t ex[4] = {excl.x, excl.y, excl.z, excl.w};
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
-      const uint32_t base = (tile * SUBS + k) * SCAN_SUB + threadIdx.x * 4u;
+      const uint32_t base = (tile * SUBS + k) * SUB + threadIdx.x * 4u;
       if (k < SUBS && base < nbuckets) {
         uint32_t run = s_base + sub_off[k] + ex[k];
         const uint4 n = ok ? c[k] : make_uint4(0u, 0u, 0u, 0u);

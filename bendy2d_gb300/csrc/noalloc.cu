@@ -110,7 +110,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   uint32_t nb = 64;
   while (nb < 2 * np) nb <<= 1;
   const uint32_t nch = (np + CHUNK - 1) / CHUNK;
-  const uint32_t nt = (nb + SCAN_SUB - 1) / SCAN_SUB;
+  const uint32_t nt = (nb + SCAN_SMALL_TILE - 1) / SCAN_SMALL_TILE;
 
   DWorld w;
   std::memset(&w, 0, sizeof(w));
@@ -155,7 +155,7 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   for (uint32_t s = 0; s < w.S; ++s) {
     const uint32_t cur = s & 1u;
     k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_grid_scan<1><<<nt, 1024, 0, st>>>(G, nb, nt);  // nt <= 32 one-sub-tile tiles
+    k_grid_scan<1, 256><<<nt, 256, 0, st>>>(G, nb, nt);  // nb <= 131072: small tiles
     k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
     k_collide_integrate<<<nch * COLLIDE_CTAS, COLLIDE_THREADS, 0, st>>>(dW, G, chunks, nch, cur, s);
   }
