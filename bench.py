@@ -274,8 +274,44 @@ def run_config5(args, torch, flush, stream):
         out[name] = {"value": v, "ms_per_step": ms,
                      "residual_after": link_residual(s, sc),
                      "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024,
-                     "roofline": step_roofline(v, step_bytes_per_unit(sc))}
+                     "roofline": step_roofline(v, step_bytes_per_unit(sc)),
+                     "kernel_rooflines": config5_kernel_rooflines(s, sc, torch, flush, stream)}
         s.close()
+    return out
+
+
+def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
+    """Per-kernel rooflines of one update at this throughput-bound size, from
+    the CUDA-event profile (each launch timed alone): the link executor
+    (every link pass of every sub-step: I x L x 44 B per sub-step) and
+    collide + bounds + integrate (32 B per particle per sub-step), against
+    the measured HBM copy bandwidth.  The link executor keeps each body in
+    shared memory through its passes, so its algorithmic bytes can exceed
+    what DRAM moves (ncu: ~41 MB read per launch)."""
+    with torch.cuda.stream(stream):
+        flush.zero_()
+    s.synchronize()
+    s.set_profiling(True)
+    s.update(sc.dt)
+    prof = s.profile()
+    s.set_profiling(False)
+    peak, kind = _peaks()
+    n, l = sc.n_particles, len(sc.la)
+    groups = {
+        "links": ([k for k in prof if k.startswith("exec_")],
+                  sc.sub_steps * sc.link_iters * l * 44.0),
+        "collide_integrate": ([k for k in prof if k == "collide_integrate"],
+                              sc.sub_steps * 32.0 * n),
+    }
+    out = {}
+    for g, (names, nbytes) in groups.items():
+        ms = sum(prof[k] for k in names)
+        if ms <= 0.0:
+            continue
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[g] = {"kernels": names, "ms_per_step": ms, "algorithmic_bytes_per_step": nbytes,
+                  "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                  "peak_source": kind}
     return out
 
 

@@ -1423,9 +1423,6 @@ __device__ __forceinline__ void visit_cell(const DGrid& G, float2 p, int32_t ncx
   }
 }
 
-// Particle collisions + bounds + integrate of one sub-step of the extension
-// pipeline.  Reads positions from buffer cur (the post-link snapshot) and
-// writes the new ones to buffer cur^1; prev is updated in place.
 // True when the interval [lo, hi] cannot reach [cmin, cmax] even allowing
 // for float rounding in the exact per-particle test (a relative margin of
 // 1e-5 is far above the few-ulp error of the subtractions and squares there).
@@ -1434,9 +1431,8 @@ __device__ __forceinline__ bool separated(float lo, float hi, float cmin, float 
   return cmax < lo - d || cmin > hi + d;
 }
 
-// min/max of the CTA's particle positions (NaN ignored)
-__device__ __forceinline__ float4 block_box(bool act, float2 p) {
-  __shared__ float4 wbox[32];
+// min/max of the warp's particle positions (NaN ignored); all 32 lanes call
+__device__ __forceinline__ float4 warp_box(bool act, float2 p) {
   float4 b = act ? make_float4(p.x, p.y, p.x, p.y)
                  : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
 #pragma unroll
@@ -1446,15 +1442,6 @@ __device__ __forceinline__ float4 block_box(bool act, float2 p) {
     b.z = fmaxf(b.z, __shfl_xor_sync(0xFFFFFFFFu, b.z, o));
     b.w = fmaxf(b.w, __shfl_xor_sync(0xFFFFFFFFu, b.w, o));
   }
-  if ((threadIdx.x & 31u) == 0) wbox[threadIdx.x >> 5] = b;
-  __syncthreads();
-  b = wbox[0];
-  for (uint32_t w = 1; w < blockDim.x / 32; ++w) {
-    const float4 c = wbox[w];
-    b.x = fminf(b.x, c.x); b.y = fminf(b.y, c.y);
-    b.z = fmaxf(b.z, c.z); b.w = fmaxf(b.w, c.w);
-  }
-  __syncthreads();
   return b;
 }
 
@@ -1468,14 +1455,14 @@ __device__ __forceinline__ float4 block_box(bool act, float2 p) {
 // split cannot change the result), then runs the circle and polygon tests,
 // bounds and integrate.  A CTA of 8 warps covers 80 particles, a quarter of
 // one work chunk (grid = 4 x chunks).  Circle and polygon tests are skipped
-// for the whole CTA when no circle or polygon box reaches the CTA's
+// for a whole warp when no circle or polygon box reaches the warp's
 // particles: then no particle is in contact, nothing moves, and so no later
 // test of the sequence can hit either — the skip is exact.
 constexpr uint32_t COLLIDE_THREADS = 256;      // 8 warps
 constexpr uint32_t COLLIDE_PER_WARP = 10;      // particles per warp, three lanes each
 constexpr uint32_t COLLIDE_CTAS = CHUNK / (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP);  // per chunk
 static_assert(COLLIDE_CTAS * (COLLIDE_THREADS / 32) * COLLIDE_PER_WARP == CHUNK, "chunk split");
-static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate(
+static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate(
     const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
   pdl_trigger();
@@ -1504,8 +1491,16 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
       const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell) + (int32_t)row - 1;  // this lane's row
       const float D = fadd(W.radius, W.radius);
       const float D2 = fmul(D, D);
-      const uint32_t b0 = bucket_of(W, cx - 1, cy), b1 = bucket_of(W, cx, cy),
-                     b2 = bucket_of(W, cx + 1, cy);
+      // bucket_of for cells cx - 1, cx, cx + 1 with two hashes: the strip of
+      // cx and the neighbouring strip that cx - 1 (first cell of its strip)
+      // or cx + 1 (last cell) falls in
+      const int32_t st = cx >> 2;
+      const uint32_t k = (uint32_t)cx & 3u;
+      const uint32_t hm = (cell_hash(st, cy) << 2) & W.gmask;
+      const uint32_t ho = (cell_hash(k == 0u ? st - 1 : st + 1, cy) << 2) & W.gmask;
+      const uint32_t b0 = W.gb0 + (k == 0u ? (ho | 3u) : (hm | (k - 1u)));
+      const uint32_t b1 = W.gb0 + (hm | k);
+      const uint32_t b2 = W.gb0 + (k == 3u ? ho : (hm | (k + 1u)));
       const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2];
       visit_cell(G, p, cx - 1, cy, r0.x, r0.y, D, D2, c);
       visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, c);
@@ -1529,10 +1524,10 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
   }
   const uint32_t flags = W.flags;
   if (flags & (COLLIDE_PC | COLLIDE_PPOLY)) {
-    const float4 box = block_box(own, p);
+    const float4 box = warp_box(own, p);
     bool near = false;
     if (flags & COLLIDE_PC) {
-      for (uint32_t k = threadIdx.x; k < W.nc; k += blockDim.x) {
+      for (uint32_t k = wl; k < W.nc; k += 32u) {
         const float2 c = W.cpos[k];
         const float R = W.radius + W.crad[k];
         near |= !(separated(c.x - R, c.x + R, box.x, box.z) ||
@@ -1540,14 +1535,14 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 4) k_collide_integrate
       }
     }
     if (flags & COLLIDE_PPOLY) {
-      for (uint32_t k = threadIdx.x; k < W.ng; k += blockDim.x) {
+      for (uint32_t k = wl; k < W.ng; k += 32u) {
         const float4 bb = W.paabb[k];
         const float r = W.radius;
         near |= !(separated(bb.x - r, bb.z + r, box.x, box.z) ||
                   separated(bb.y - r, bb.w + r, box.y, box.w));
       }
     }
-    if (__syncthreads_or(near) && own) {
+    if (__any_sync(0xFFFFFFFFu, near) && own) {
       if (flags & COLLIDE_PC) p = particle_circles(W, p);
       if (flags & COLLIDE_PPOLY) {
         for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
