@@ -64,7 +64,8 @@ struct DSched {
   uint32_t chunk0, nchunks;  // chunk_off / chunk_len entries
   uint32_t nlvl, nops;
   uint32_t off, words;       // the chunks are contiguous: stream[off, off + words)
-  uint32_t len0, pad;        // words of the first chunk
+  uint32_t len0;             // words of the first chunk
+  uint32_t maxw;             // most ops in one segment
 };
 
 // 1 / c when c is a positive normal power of two (then x / c == x * (1/c)

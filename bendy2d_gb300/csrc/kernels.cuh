@@ -8,6 +8,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "b2d_dev.h"
 
@@ -374,25 +375,53 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   };
   // One chunk at shared address buf_a: its segments in order, each followed
   // by the group barrier; a segment's ops go to the group's threads in turn.
-  // (Prefetching the next segment's op ahead of the barrier measured slower
-  // than this plain form.)  Returns the address just past the chunk.
-  auto run_chunk = [&](uint32_t buf_a) {
+  // The segment ends come from registers, not shared memory: each warp
+  // (a group is whole warps) loads 32 ends at a time, lane i holding end i,
+  // and takes the next segment's end by shuffle before the barrier, so after
+  // the barrier a thread's first load is its op.  (A shared-memory load of
+  // the end there sat on every level's dependency chain; prefetching the
+  // next op by a shared load ahead of the barrier measured slower.)
+  // Returns the address just past the chunk.  ONE: a CTA of one group whose
+  // segments are no wider than the group (one op per thread at most, the
+  // CTA barrier), decided once per launch so the level loop carries neither
+  // the op loop nor the barrier choice.
+  auto run_chunk = [&](uint32_t buf_a, auto one) {
+    constexpr bool ONE = decltype(one)::value;
     const uint32_t nseg = lds_u32(buf_a);
     const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
+    const uint32_t lane = threadIdx.x & 31u;
     uint32_t beg = 0;
-    for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
-      const uint32_t end = lds_u32(buf_a + 4u + 4u * sgi);
-      for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
-      group_sync(g, T);
-      beg = end;
+    for (uint32_t s0 = 0; s0 < nseg; s0 += 32u) {
+      const uint32_t n = min(32u, nseg - s0);  // uniform over the group
+      const uint32_t my_end = lane < n ? lds_u32(buf_a + 4u + 4u * (s0 + lane)) : 0u;
+      uint32_t end = __shfl_sync(0xFFFFFFFFu, my_end, 0);
+      for (uint32_t j = 0; j < n; ++j) {
+        if constexpr (ONE) {
+          if (beg + t < end) run(lds_u32x2(ops_a + 8u * (beg + t)));
+        } else {
+          for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
+        }
+        const uint32_t next = __shfl_sync(0xFFFFFFFFu, my_end, (j + 1u) & 31u);
+        if constexpr (ONE) {
+          __syncthreads();
+        } else {
+          group_sync(g, T);
+        }
+        beg = end;
+        end = next;
+      }
     }
     return (ops_a + 8u * beg + 15u) & ~15u;  // chunks are padded to 16 bytes
+  };
+  const bool one = T == blockDim.x && S.maxw <= T;
+  auto walk = [&](uint32_t buf_a) {
+    return one ? run_chunk(buf_a, std::true_type{}) : run_chunk(buf_a, std::false_type{});
   };
 
   const uint32_t cbuf_a = smem_addr(cbuf);
   if (RES) {
     uint32_t buf_a = cbuf_a;
-    for (uint32_t c = 0; c < S.nchunks; ++c) buf_a = run_chunk(buf_a);
+    for (uint32_t c = 0; c < S.nchunks; ++c) buf_a = walk(buf_a);
   } else {
     // buffer k2 = f & 1 holds fill f, used for the (f >> 1)-th time: its
     // mbarrier phase parity is (f >> 1) & 1
@@ -416,7 +445,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
         next_c = issue_fill(next_c, k2 ^ 1u);
       }
       uint32_t buf_a = cbuf_a + k2 * fill_words * 4u;
-      for (uint32_t j = 0; j < n; ++j) buf_a = run_chunk(buf_a);
+      for (uint32_t j = 0; j < n; ++j) buf_a = walk(buf_a);
       c += n;
     }
   }

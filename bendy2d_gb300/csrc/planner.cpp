@@ -150,7 +150,8 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   }
   flush();
   d.nchunks = (uint32_t)chunk_off.size() - d.chunk0;
-  d.off = d.words = d.len0 = d.pad = 0;
+  d.off = d.words = d.len0 = d.maxw = 0;
+  for (uint32_t l = 1; l <= maxl; ++l) d.maxw = std::max(d.maxw, start[l + 1] - start[l]);
   if (d.nchunks) {
     d.off = chunk_off[d.chunk0];
     d.len0 = chunk_len[d.chunk0];
