@@ -381,12 +381,13 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   // the barrier a thread's first load is its op.  (A shared-memory load of
   // the end there sat on every level's dependency chain; prefetching the
   // next op by a shared load ahead of the barrier measured slower.)
-  // Returns the address just past the chunk.  ONE: a CTA of one group whose
-  // segments are no wider than the group (one op per thread at most, the
-  // CTA barrier), decided once per launch so the level loop carries neither
-  // the op loop nor the barrier choice.
-  auto run_chunk = [&](uint32_t buf_a, auto one) {
+  // Returns the address just past the chunk.  ONE: segments no wider than
+  // the group (one op per thread at most); KIND: the group barrier (0 warp,
+  // 1 CTA, 2 named).  Both are decided once per launch, so the level loop
+  // carries neither the op loop nor the barrier choice.
+  auto run_chunk = [&](uint32_t buf_a, auto one, auto kind) {
     constexpr bool ONE = decltype(one)::value;
+    constexpr int KIND = decltype(kind)::value;
     const uint32_t nseg = lds_u32(buf_a);
     const uint32_t ops_a = buf_a + 4u * ((2u + nseg) & ~1u);
     const uint32_t lane = threadIdx.x & 31u;
@@ -402,10 +403,12 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
           for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
         }
         const uint32_t next = __shfl_sync(0xFFFFFFFFu, my_end, (j + 1u) & 31u);
-        if constexpr (ONE) {
+        if constexpr (KIND == 0) {
+          __syncwarp();
+        } else if constexpr (KIND == 1) {
           __syncthreads();
         } else {
-          group_sync(g, T);
+          asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(T) : "memory");
         }
         beg = end;
         end = next;
@@ -413,9 +416,20 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     }
     return (ops_a + 8u * beg + 15u) & ~15u;  // chunks are padded to 16 bytes
   };
-  const bool one = T == blockDim.x && S.maxw <= T;
+  const bool one = S.maxw <= T;
+  const int kind = T == 32 ? 0 : (T == blockDim.x ? 1 : 2);  // as group_sync
   auto walk = [&](uint32_t buf_a) {
-    return one ? run_chunk(buf_a, std::true_type{}) : run_chunk(buf_a, std::false_type{});
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    if (one) {
+      return kind == 1 ? run_chunk(buf_a, std::true_type{}, I1{})
+             : kind == 0 ? run_chunk(buf_a, std::true_type{}, I0{})
+                         : run_chunk(buf_a, std::true_type{}, I2{});
+    }
+    return kind == 1 ? run_chunk(buf_a, std::false_type{}, I1{})
+           : kind == 0 ? run_chunk(buf_a, std::false_type{}, I0{})
+                       : run_chunk(buf_a, std::false_type{}, I2{});
   };
 
   const uint32_t cbuf_a = smem_addr(cbuf);
