@@ -375,16 +375,19 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   };
   // One chunk at shared address buf_a: its segments in order, each followed
   // by the group barrier; a segment's ops go to the group's threads in turn.
-  // The segment ends come from registers, not shared memory: each warp
-  // (a group is whole warps) loads 32 ends at a time, lane i holding end i,
-  // and takes the next segment's end by shuffle before the barrier, so after
-  // the barrier a thread's first load is its op.  (A shared-memory load of
-  // the end there sat on every level's dependency chain; prefetching the
-  // next op by a shared load ahead of the barrier measured slower.)
-  // Returns the address just past the chunk.  ONE: segments no wider than
-  // the group (one op per thread at most); KIND: the group barrier (0 warp,
-  // 1 CTA, 2 named).  Both are decided once per launch, so the level loop
-  // carries neither the op loop nor the barrier choice.
+  // Returns the address just past the chunk.
+  //
+  // Every level is one dependency chain (barrier, op, positions, link solve,
+  // stores, barrier), so the loop keeps everything else off it:
+  // * ONE (no segment wider than the group): one predicated op per thread
+  //   instead of an op loop;
+  // * KIND, the group barrier (0 warp, 1 CTA, 2 named), fixed at compile
+  //   time; ONE and KIND are chosen once per launch (`walk`);
+  // * the segment ends sit in registers (a group is whole warps: lane i
+  //   holds the end of segment s0 + i) and the next end is taken by shuffle
+  //   before the barrier, so after it a thread's first load is its op.
+  // A shared-memory prefetch of the next op ahead of the barrier measured
+  // slower.
   auto run_chunk = [&](uint32_t buf_a, auto one, auto kind) {
     constexpr bool ONE = decltype(one)::value;
     constexpr int KIND = decltype(kind)::value;
