@@ -203,6 +203,17 @@ int Engine::fill_world_record(uint32_t slot) {
 }
 
 int Engine::add(WorldHost* w, uint32_t* out_slot, std::string* why) {
+  WorldImage img;
+  const int st = plan(*w, &img, why);
+  if (st != OK) return st;
+  return add_planned(w, std::move(img), out_slot);
+}
+
+int Engine::plan(const WorldHost& w, WorldImage* img, std::string* why) {
+  return plan_world(w, tune_, reg_, *img, why);
+}
+
+int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
   uint32_t slot;
   if (!free_slots_.empty()) {
     slot = free_slots_.back();
@@ -212,11 +223,7 @@ int Engine::add(WorldHost* w, uint32_t* out_slot, std::string* why) {
     slots_.emplace_back();
   }
   Slot& s = slots_[slot];
-  int st = plan_world(*w, tune_, reg_, s.img, why);
-  if (st != OK) {
-    free_slots_.push_back(slot);
-    return st;
-  }
+  s.img = std::move(img);
   s.host = w;
   s.L = layout_of(s.img);
   B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&s.block), s.L.total, stream_));
@@ -225,7 +232,7 @@ int Engine::add(WorldHost* w, uint32_t* out_slot, std::string* why) {
   write_block(s.img, s.L, stage.data());
   B2D_CUDA(cudaMemcpyAsync(s.block, stage.data(), s.L.total, cudaMemcpyHostToDevice, stream_));
   s.live = true;
-  st = fill_world_record(slot);
+  const int st = fill_world_record(slot);
   if (st != OK) return st;
   B2D_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is pageable
   lists_dirty_ = true;

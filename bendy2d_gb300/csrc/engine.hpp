@@ -116,6 +116,12 @@ class Engine {
   Engine& operator=(const Engine&) = delete;
 
   int add(WorldHost* w, uint32_t* slot, std::string* why);
+  // add() in two parts: plan() is host work only (it may run while launched
+  // work of this engine is in flight; it grows the host side of the schedule
+  // registry, which the next step uploads), add_planned() allocates, uploads
+  // and registers the world; the image is consumed
+  int plan(const WorldHost& w, WorldImage* img, std::string* why);
+  int add_planned(WorldHost* w, WorldImage&& img, uint32_t* slot);
   int remove(uint32_t slot);
   int set_dt(uint32_t slot, float dt);
   int set_params(uint32_t slot);          // gravity / bounds changed on the host mirror

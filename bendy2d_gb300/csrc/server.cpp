@@ -2,14 +2,17 @@
 //
 // A request is a world (a copy of a solver's contents) plus a number of
 // Solver::update calls.  A worker thread repeats one tick:
-//   1. admit queued requests, first come first served, while the device bytes
-//      of the resident worlds plus the candidate stay within the budget;
-//   2. one Solver::update for every resident world, all in one launch sequence
-//      of a shared Engine (the same batched kernels as b2d_batch_update);
-//   3. retire requests that reached their step count: copy the state back,
-//      free the world's device block, record the latency.
-// Requests that arrive while a tick runs wait in the queue and join at the
-// next tick, so work overlaps on the device as memory frees up.  World state
+//   1. take queued requests, first come first served, while the device bytes
+//      of the resident worlds plus the candidate stay within the budget, and
+//      install (upload) the ones planned during the previous tick;
+//   2. launch one Solver::update for every resident world, all in one launch
+//      sequence of a shared Engine (the same batched kernels as
+//      b2d_batch_update), and plan the requests taken in step 1 on the host
+//      while it runs;
+//   3. wait, then retire requests that reached their step count: copy the
+//      state back, free the world's device block, record the latency.
+// Requests that arrive while a tick runs wait in the queue and join within
+// two ticks, so work overlaps on the device as memory frees up.  World state
 // stays device-resident across ticks.  Every world is computed independently
 // (per-world grids, order-independent sums), so a result is bit-identical
 // whether the request ran alone or in a mix.
@@ -157,40 +160,70 @@ ServerStats Server::stats() {
 
 void Server::loop() {
   std::unique_ptr<Engine> eng;
+  // requests taken from the queue and planned during the last tick, waiting
+  // to be installed after it
+  std::vector<std::pair<Req*, WorldImage>> planned;
+  auto fail = [&](Req* r, const std::string& why) {
+    std::lock_guard<std::mutex> lk(mu_);
+    r->t_admit = Clock::now();
+    r->state = SERVE_FAILED;
+    r->error = why;
+    resident_ -= r->bytes;
+    ++stats_.failed;
+    finished_.push_back(r->id);
+  };
+  auto plan = [&](Req* r) {
+    WorldImage img;
+    std::string why;
+    const int st = eng->plan(r->world, &img, &why);
+    if (st != OK) fail(r, why.empty() ? eng->last_error : why);
+    else planned.emplace_back(r, std::move(img));
+  };
   for (;;) {
-    std::vector<Req*> admit;
+    std::vector<Req*> taken;
     {
       std::unique_lock<std::mutex> lk(mu_);
-      cv_.wait(lk, [&] { return !running_ || !queue_.empty() || !active_.empty(); });
+      cv_.wait(lk, [&] {
+        return !running_ || !queue_.empty() || !active_.empty() || !planned.empty();
+      });
       if (!running_) break;
       // first come, first served while the budget holds
       while (!queue_.empty() && resident_ + queue_.front()->bytes <= budget_) {
         Req* r = queue_.front();
         queue_.pop_front();
         resident_ += r->bytes;
-        admit.push_back(r);
+        taken.push_back(r);
       }
     }
     if (!eng) eng = std::make_unique<Engine>(nullptr);
     const Clock::time_point ta = Clock::now();
-    for (Req* r : admit) {
-      std::string why;
-      int st = eng->add(&r->world, &r->slot, &why);
-      if (st == OK) st = eng->set_dt(r->slot, r->dt);
+    // with nothing on the device there is no tick to plan under: plan now
+    bool idle;
+    {
       std::lock_guard<std::mutex> lk(mu_);
-      r->t_admit = Clock::now();
+      idle = active_.empty();
+    }
+    if (idle) {
+      for (Req* r : taken) plan(r);
+      taken.clear();
+    }
+    for (auto& pr : planned) {
+      Req* r = pr.first;
+      uint32_t slot = 0;
+      int st = eng->add_planned(&r->world, std::move(pr.second), &slot);
+      if (st == OK) st = eng->set_dt(slot, r->dt);
       if (st != OK) {
-        r->state = SERVE_FAILED;
-        r->error = why.empty() ? eng->last_error : why;
-        resident_ -= r->bytes;
-        ++stats_.failed;
-        finished_.push_back(r->id);
+        fail(r, eng->last_error);
         continue;
       }
+      std::lock_guard<std::mutex> lk(mu_);
+      r->slot = slot;
+      r->t_admit = Clock::now();
       r->state = SERVE_RUNNING;
       active_.push_back(r);
       ++stats_.admitted;
     }
+    planned.clear();
     std::vector<Req*> act;
     const Clock::time_point ts = Clock::now();
     {
@@ -198,15 +231,20 @@ void Server::loop() {
       act = active_;
       stats_.admit_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(ts - ta).count();
     }
-    if (act.empty()) continue;
+    if (act.empty()) {
+      for (Req* r : taken) plan(r);
+      continue;
+    }
     // requests that asked for zero steps finish without a tick
     int st = OK;
     bool any_steps = false;
     for (Req* r : act) any_steps |= r->done < r->steps;
-    if (any_steps) {
-      st = eng->step();
-      if (st == OK) st = eng->sync();
-    }
+    if (any_steps) st = eng->step();
+    // the requests taken this tick are planned on the host while it runs
+    const Clock::time_point tp = Clock::now();
+    for (Req* r : taken) plan(r);
+    const Clock::time_point tq = Clock::now();
+    if (any_steps && st == OK) st = eng->sync();
     const Clock::time_point tr = Clock::now();
     uint64_t units = 0;
     std::vector<Req*> finished;
@@ -238,9 +276,14 @@ void Server::loop() {
     std::lock_guard<std::mutex> lk(mu_);
     ++stats_.ticks;
     stats_.particle_substeps += units;
-    stats_.step_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(tr - ts).count();
+    // planning under the tick counts as admission, the rest of the tick as
+    // stepping
+    stats_.admit_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(tq - tp).count();
+    stats_.step_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>((tr - ts) - (tq - tp)).count();
     stats_.retire_ns += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(te - tr).count();
   }
+  // requests planned but never installed are released
+  for (auto& pr : planned) fail(pr.first, "server stopped");
   eng.reset();
 }
 
