@@ -137,3 +137,32 @@ def test_solver_methods_of_the_reference_are_bound():
         assert re.search(rf"pub fn {f}\(", src), f
     for field in ("gravity", "bounds", "bounds_active"):
         assert re.search(rf"pub {field}:", src), field
+
+
+def test_value_type_methods_of_the_reference_are_bound():
+    """The public methods of the reference's value types and its free
+    functions: src/particle.rs:11-59, src/circle.rs:10-45, src/link.rs:17-48,
+    src/polygon.rs:16-229, src/common.rs:3-52."""
+    expect = {
+        "particle.rs": ["new", "update", "solve_bounds", "add_force", "add_force_v2",
+                        "add_force_towards"],
+        "circle.rs": ["solve_bounds", "solve_circle"],
+        "link.rs": ["solve"],
+        "polygon.rs": ["circle", "new", "update", "solve_bounds", "solve_polygon",
+                       "solve_polygon_single", "solve_links", "add_force_v2"],
+        "common.rs": ["line_intersection", "proj_a_on_b", "proj_a_on_b_clamped",
+                      "proj_point_on_line"],
+    }
+    for f, names in expect.items():
+        src = (CRATE / "src" / f).read_text()
+        for n in names:
+            assert re.search(rf"pub fn {n}\(", src), (f, n)
+    link = (CRATE / "src" / "link.rs").read_text()
+    assert link.count("pub fn solve(") == 2  # ParticleLink and CircleLink
+    for ty, fields in (("particle.rs", ["pos", "prev_pos"]), ("circle.rs", ["point", "radius"]),
+                       ("link.rs", ["particle_a", "particle_b", "target_distance", "link"]),
+                       ("polygon.rs", ["particles", "particle_links", "is_static", "center",
+                                       "scale"])):
+        src = (CRATE / "src" / ty).read_text()
+        for fl in fields:
+            assert re.search(rf"pub {fl}:", src), (ty, fl)
