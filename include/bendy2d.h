@@ -211,7 +211,9 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
  * calls (src/solver.rs:106-116).  A worker thread admits queued requests
  * first come first served while the device bytes of resident worlds stay
  * within the budget, steps every resident world once per tick in one launch
- * sequence, and retires finished requests.  Results are bit-identical to
+ * sequence, and retires finished requests.  A request taken from the queue
+ * is planned on the host while the current tick runs and joins the next
+ * one (it stays B2D_SERVE_QUEUED until then).  Results are bit-identical to
  * running the request alone. */
 #define B2D_SERVE_QUEUED 0
 #define B2D_SERVE_RUNNING 1
@@ -220,8 +222,9 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
 typedef struct {
   uint64_t submitted, admitted, completed, failed, queued, active;
   uint64_t ticks, particle_substeps, resident_bytes;
-  /* worker wall time, nanoseconds: admitting (planning + upload), stepping
-   * (launch + wait), retiring (download + release) */
+  /* worker wall time, nanoseconds: admitting (planning, also while a tick
+   * runs, + upload), stepping (launch + wait, minus that planning), retiring
+   * (download + release) */
   uint64_t admit_ns, step_ns, retire_ns;
 } b2d_server_stats;
 int b2d_server_create(uint64_t budget_bytes, b2d_server** out);
