@@ -30,6 +30,36 @@ def _v(p) -> tuple:
     return (float(p[0]), float(p[1]))
 
 
+# Host arithmetic of the per-object methods: float32, one rounding per
+# operation, in the reference's order (nalgebra: norm = sqrt(x*x + y*y),
+# normalize = componentwise division by the norm).
+_F = np.float32
+
+
+def _f2(p) -> tuple:
+    return (_F(p[0]), _F(p[1]))
+
+
+def _py(p) -> tuple:
+    return (float(p[0]), float(p[1]))
+
+
+def _norm(x, y):
+    return np.sqrt(x * x + y * y)
+
+
+def _reflect(pos, prev, lo, hi):
+    """One axis of solve_bounds: below lo, else above hi, the coordinate is
+    put on the bound and the Verlet velocity reflected."""
+    if pos < lo:
+        v = prev - pos
+        return lo, lo - v
+    if pos > hi:
+        v = prev - pos
+        return hi, hi - v
+    return pos, prev
+
+
 @dataclass
 class Particle:
     """src/particle.rs:4-9 (``acc`` is private there; exposed read-only here)."""
@@ -42,6 +72,36 @@ class Particle:
         p = _v(pos)
         return Particle(p, p, (0.0, 0.0))
 
+    def update(self, dt: float) -> None:
+        """src/particle.rs:20-25: pos + velocity + (acc * dt) * dt."""
+        (x, y), (qx, qy), (ax, ay), d = _f2(self.pos), _f2(self.prev_pos), _f2(self.acc), _F(dt)
+        vx, vy = x - qx, y - qy
+        self.prev_pos = _py((x, y))
+        self.pos = _py(((x + vx) + (ax * d) * d, (y + vy) + (ay * d) * d))
+        self.acc = (0.0, 0.0)
+
+    def solve_bounds(self, bounds: "Bounds") -> None:
+        """src/particle.rs:27-46."""
+        (x, y), (qx, qy) = _f2(self.pos), _f2(self.prev_pos)
+        (bx, by), (bw, bh) = _f2(bounds.pos), _f2(bounds.size)
+        x, qx = _reflect(x, qx, bx, bx + bw)
+        y, qy = _reflect(y, qy, by, by + bh)
+        self.pos, self.prev_pos = _py((x, y)), _py((qx, qy))
+
+    def add_force(self, force_x: float, force_y: float) -> None:  # src/particle.rs:48-50
+        self.add_force_v2((force_x, force_y))
+
+    def add_force_v2(self, force) -> None:  # src/particle.rs:52-54
+        (ax, ay), (fx, fy) = _f2(self.acc), _f2(force)
+        self.acc = _py((ax + fx, ay + fy))
+
+    def add_force_towards(self, point, force: float) -> None:
+        """src/particle.rs:56-59: along the unit vector towards point."""
+        (px, py), (x, y), f = _f2(point), _f2(self.pos), _F(force)
+        dx, dy = px - x, py - y
+        n = _norm(dx, dy)
+        self.add_force_v2((dx / n * f, dy / n * f))
+
 
 @dataclass
 class Link:
@@ -52,14 +112,53 @@ class Link:
     stiffness: float = 1.0  # extension; 1.0 reproduces the reference
 
 
+def _link_ends(seq, link: Link):
+    """The two elements of a link; the reference indexes them through
+    split_at_mut and panics unless particle_a < particle_b < len
+    (src/link.rs:19-21)."""
+    a, b = link.particle_a, link.particle_b
+    if not (0 <= a < b < len(seq)):
+        raise IndexError(f"link ({a}, {b}) needs a < b < {len(seq)}")
+    return seq[a], seq[b]
+
+
 @dataclass
 class ParticleLink:  # src/link.rs:12-15
     link: Link
+
+    def solve(self, particles: list) -> None:
+        """src/link.rs:18-27 (the stiffness extension multiplies last; 1.0 is
+        exact)."""
+        pa, pb = _link_ends(particles, self.link)
+        (ax, ay), (bx, by) = _f2(pa.pos), _f2(pb.pos)
+        t, k = _F(self.link.target_distance), _F(self.link.stiffness)
+        dx, dy = ax - bx, ay - by
+        dist = _norm(dx, dy)
+        nx, ny = dx / dist, dy / dist
+        m = dist - t
+        cx, cy = nx * m * _F(0.5) * k, ny * m * _F(0.5) * k
+        pa.pos = _py((ax - cx, ay - cy))
+        pb.pos = _py((bx + cx, by + cy))
 
 
 @dataclass
 class CircleLink:  # src/link.rs:30-33
     link: Link
+
+    def solve(self, circles: list) -> None:
+        """src/link.rs:36-48: the correction split by the squared radii."""
+        ca, cb = _link_ends(circles, self.link)
+        (ax, ay), (bx, by) = _f2(ca.point.pos), _f2(cb.point.pos)
+        t = _F(self.link.target_distance)
+        dx, dy = ax - bx, ay - by
+        dist = _norm(dx, dy)
+        nx, ny = dx / dist, dy / dist
+        ra, rb = _F(ca.radius), _F(cb.radius)
+        ra2, rb2 = ra * ra, rb * rb
+        scale = _F(1.0) / (ra2 + rb2)
+        m = dist - t
+        ca.point.pos = _py((ax - nx * m * scale * rb2, ay - ny * m * scale * rb2))
+        cb.point.pos = _py((bx + nx * m * scale * ra2, by + ny * m * scale * ra2))
 
 
 @dataclass
@@ -67,6 +166,33 @@ class Circle:  # src/circle.rs:4-8
     point: Particle
     radius: float
     is_static: bool = False  # extension
+
+    def solve_bounds(self, bounds: "Bounds") -> None:
+        """src/circle.rs:11-30: the particle rule with the bounds shrunk by
+        the radius."""
+        (x, y), (qx, qy) = _f2(self.point.pos), _f2(self.point.prev_pos)
+        (bx, by), (bw, bh), r = _f2(bounds.pos), _f2(bounds.size), _F(self.radius)
+        x, qx = _reflect(x, qx, bx + r, bx + bw - r)
+        y, qy = _reflect(y, qy, by + r, by + bh - r)
+        self.point.pos, self.point.prev_pos = _py((x, y)), _py((qx, qy))
+
+    def solve_circle(self, circle: "Circle") -> None:
+        """src/circle.rs:32-45: overlapping discs pushed apart, each by the
+        other's share of the squared radii."""
+        (ax, ay), (bx, by) = _f2(self.point.pos), _f2(circle.point.pos)
+        ra, rb = _F(self.radius), _F(circle.radius)
+        dx, dy = ax - bx, ay - by
+        d2 = dx * dx + dy * dy
+        rs = ra + rb
+        if d2 < rs * rs:
+            n = _norm(dx, dy)
+            nx, ny = dx / n, dy / n
+            overlap = rs - np.sqrt(d2)
+            ra2, rb2 = ra * ra, rb * rb
+            scale = _F(1.0) / (ra2 + rb2)
+            self.point.pos = _py((ax + nx * scale * overlap * rb2, ay + ny * scale * overlap * rb2))
+            circle.point.pos = _py((bx - nx * scale * overlap * ra2,
+                                    by - ny * scale * overlap * ra2))
 
 
 @dataclass
@@ -98,6 +224,137 @@ class Polygon:  # src/polygon.rs:7-14
         pts = (N.Vec2 * len(points))(*[N.Vec2(*_v(p)) for p in points])
         s._chk(s._lib.b2d_add_polygon_points(s._h, len(points), pts, int(is_static)))
         return s.get_polygon(0)
+
+    def update(self, dt: float) -> None:
+        """src/polygon.rs:125-134: centre, then every vertex, unless static."""
+        if self.is_static:
+            return
+        self._calc_center()
+        for p in self.particles:
+            p.update(dt)
+
+    def solve_bounds(self, bounds: Bounds) -> None:  # src/polygon.rs:136-140
+        for p in self.particles:
+            p.solve_bounds(bounds)
+
+    def solve_polygon(self, other: "Polygon") -> None:  # src/polygon.rs:142-145
+        self.solve_polygon_single(other)
+        other.solve_polygon_single(self)
+
+    def solve_polygon_single(self, other: "Polygon") -> None:
+        """src/polygon.rs:147-162: every edge (i, i+1) against every vertex
+        of other; the edge's end points are copied when the edge starts and
+        the copies serve all of other's vertices, while each hit writes both
+        end points and the vertex."""
+        n = len(self.particles)
+        for i in range(n):
+            j = (i + 1) % n
+            a, b = _f2(self.particles[i].pos), _f2(self.particles[j].pos)
+            for q in other.particles:
+                hit = _edge_contact(_f2(self.center), a, b, _f2(q.pos), _f2(other.center))
+                if hit is not None:
+                    self.particles[i].pos, self.particles[j].pos, q.pos = (_py(v) for v in hit)
+
+    def solve_links(self) -> None:  # src/polygon.rs:218-223
+        self._calc_center()
+        for link in self.particle_links:
+            link.solve(self.particles)
+
+    def add_force_v2(self, force) -> None:  # src/polygon.rs:225-229
+        for p in self.particles:
+            p.add_force_v2(force)
+
+    def _calc_center(self) -> None:
+        """src/polygon.rs:231-237: summed from zero in vertex order, then
+        divided by the count."""
+        cx, cy = _F(0.0), _F(0.0)
+        for p in self.particles:
+            px, py = _f2(p.pos)
+            cx, cy = cx + px, cy + py
+        k = _F(len(self.particles))
+        self.center = _py((cx / k, cy / k))
+
+
+def _edge_contact(center, a, b, q, other_center):
+    """src/polygon.rs:164-216: vertex q of a polygon with centre
+    other_center against edge a-b of a polygon with centre `center`.  The
+    segment q-other_center must cross the edge; the edge then moves two
+    thirds of q's depth along the edge's inward normal, shared by a and b in
+    proportion to the crossing's distance from the other end, and q moves to
+    where a ray from it against that normal (length 10000) crosses the old
+    edge.  None when either crossing is missing."""
+    hit = line_intersection((a, b), (q, other_center))
+    if hit is None:
+        return None
+    hx, hy = _f2(hit)
+    ex, ey = b[0] - a[0], b[1] - a[1]
+    en = _norm(ex, ey)
+    ux, uy = ex / en, ey / en
+    cx, cy = center[0] - hx, center[1] - hy
+    s = (ux * cx + uy * cy) / (ux * ux + uy * uy)
+    px, py = s * ux, s * uy
+    ix, iy = center[0] - (hx + px), center[1] - (hy + py)
+    inn = _norm(ix, iy)
+    nx, ny = ix / inn, iy / inn
+    to_a = _norm(hx - a[0], hy - a[1])
+    to_b = _norm(hx - b[0], hy - b[1])
+    length = to_a + to_b
+    share_a, share_b = to_b / length, to_a / length
+    dx, dy = hx - q[0], hy - q[1]
+    t = (nx * dx + ny * dy) / (nx * nx + ny * ny)
+    ox, oy = t * nx, t * ny
+    mx, my = ox / _F(3.0) * _F(2.0), oy / _F(3.0) * _F(2.0)
+    new_a = (a[0] - share_a * mx, a[1] - share_a * my)
+    new_b = (b[0] - share_b * mx, b[1] - share_b * my)
+    far = (q[0] - nx * _F(10000.0), q[1] - ny * _F(10000.0))
+    new_q = line_intersection((a, b), (q, far))
+    if new_q is None:
+        return None
+    return new_a, new_b, _f2(new_q)
+
+
+def line_intersection(line1, line2):
+    """common::line_intersection, src/common.rs:3-26: parameters s (along
+    line2) and t (along line1) in [0, 1] give p1 + t * (p2 - p1); parallel
+    segments give a non-finite s or t and no hit.  f32, the reference's
+    operation order (the denominator is evaluated twice)."""
+    (p1, p2), (p3, p4) = (_f2(line1[0]), _f2(line1[1])), (_f2(line2[0]), _f2(line2[1]))
+    s1x, s1y = p2[0] - p1[0], p2[1] - p1[1]
+    s2x, s2y = p4[0] - p3[0], p4[1] - p3[1]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = (-s1y * (p1[0] - p3[0]) + s1x * (p1[1] - p3[1])) / (-s2x * s1y + s1x * s2y)
+        t = (s2x * (p1[1] - p3[1]) - s2y * (p1[0] - p3[0])) / (-s2x * s1y + s1x * s2y)
+    if _F(0.0) <= s <= _F(1.0) and _F(0.0) <= t <= _F(1.0):
+        return _py((p1[0] + t * s1x, p1[1] + t * s1y))
+    return None
+
+
+def proj_a_on_b(a, b):
+    """common::proj_a_on_b, src/common.rs:28-32: a.dot(b) / |b|^2 * b."""
+    (ax, ay), (bx, by) = _f2(a), _f2(b)
+    k = (ax * bx + ay * by) / (bx * bx + by * by)
+    return _py((k * bx, k * by))
+
+
+def proj_a_on_b_clamped(a, b):
+    """common::proj_a_on_b_clamped, src/common.rs:34-44: the projection,
+    replaced by b when it is greater than b in every component and by zero
+    when it is less than zero in every component (nalgebra's component-wise
+    vector comparison)."""
+    p = _f2(proj_a_on_b(a, b))
+    bb = _f2(b)
+    if p[0] > bb[0] and p[1] > bb[1]:
+        return _py(bb)
+    if p[0] < 0 and p[1] < 0:
+        return (0.0, 0.0)
+    return _py(p)
+
+
+def proj_point_on_line(point, line):
+    """common::proj_point_on_line, src/common.rs:46-52."""
+    (sx, sy), (ex, ey), (px, py) = _f2(line[0]), _f2(line[1]), _f2(point)
+    q = _f2(proj_a_on_b_clamped((px - sx, py - sy), (ex - sx, ey - sy)))
+    return _py((sx + q[0], sy + q[1]))
 
 
 def _cpart(p: Particle) -> N.CParticle:
