@@ -107,20 +107,28 @@ def build_scene(seed: int = 0):
     return scenes.config2(seed=seed)
 
 
+def config_dict(sc, world: int) -> dict:
+    """The workload description both arms print (identical by design)."""
+    return {"workload": WORKLOAD, "particles": sc.n_particles, "links": int(len(sc.la)),
+            "sub_steps": sc.sub_steps, "link_iters": sc.link_iters,
+            "mode": "reference-order", "collisions": "pp+pc+ppoly",
+            "l2": "flushed (256 MiB write) between timed steps",
+            "parallelism": f"replicas x{world}"}
+
+
 def algorithmic_bytes(kernel: str, sc) -> float:
-    """Algorithmic HBM bytes of one launch (per-unit figures: 32 B per
-    particle for bounds+integrate; (12 + 32) B per link per iteration for a
-    link pass: endpoints ab + rest, then read+write of both positions)."""
-    n, l = sc.n_particles, len(sc.la)
-    if kernel.startswith("exec_groups_links") or kernel == "exec_serial_links":
-        return sc.link_iters * l * 44.0
+    """Algorithmic bytes of one launch of a kernel of the profile
+    (kernel_byte_models); a whole-step executor launch (worlds without
+    collisions) covers every sub-step: links and 32 B of bounds+integrate per
+    particle each."""
+    m = kernel_byte_models(sc)
     if kernel.startswith("exec_groups_full") or kernel == "exec_serial_full":
-        return sc.sub_steps * (sc.link_iters * l * 44.0 + 32.0 * n)
-    if kernel == "collide_integrate":
-        return 32.0 * n
-    if kernel == "grid_insert":
-        return 8.0 * n + 4.0 * n + 16.0 * n
-    return 0.0
+        return sc.sub_steps * (m["links"][0] + 32.0 * sc.n_particles)
+    if kernel.startswith("exec_"):
+        return m["links"][0]
+    if kernel.startswith("rigid"):
+        return m["rigid"][0]
+    return m[kernel][0] if kernel in m else 0.0
 
 
 def step_bytes_per_unit(sc) -> float:
@@ -244,6 +252,103 @@ def link_residual(solver, sc) -> dict:
             "median": float(np.median(r))}
 
 
+def energy(pos, prev, h: float, g) -> float:
+    """Total energy per unit mass of the solver particles, in float64:
+    sum of 1/2 |(pos - prev) / h|^2 (the Verlet velocity of
+    src/particle.rs:20-25 over one sub-step) minus g . pos."""
+    p = pos.astype(np.float64)
+    v = (p - prev.astype(np.float64)) / h
+    return float(0.5 * np.sum(v * v) - np.sum(p @ np.asarray(g, np.float64)))
+
+
+def residual_of(pos, sc) -> np.ndarray:
+    """|len - rest| / rest of every particle link (float64)"""
+    a, b = sc.la.astype(np.int64), sc.lb.astype(np.int64)
+    d = np.linalg.norm(pos[a].astype(np.float64) - pos[b], axis=1)
+    return np.abs(d - sc.rest) / sc.rest
+
+
+def run_config1_long(args, torch, stream) -> dict:
+    """Configuration 1 over its full run (600 updates of the 32x32 cloth,
+    reference semantics): the GPU against the CPU port of the reference, bit
+    parity at the last step, and the long-run statistics (constraint residual
+    and total-energy drift per step) in reference order and in the fast
+    coloured order."""
+    from bendy2d_gb300 import MODE_FAST, MODE_REFERENCE, scenes
+    from oracle import load_scene
+    steps = args.config1_steps
+    out = {"workload": "32x32 cloth (1,024 particles, 3,906 links), 4 static circles, static "
+                       f"floor polygon, 8 sub-steps, 4 link iterations, {steps} updates",
+           "steps": steps}
+    marks = sorted({1, 10, 100, steps // 2, steps} & set(range(1, steps + 1)))
+    for name, mode in (("reference_order", MODE_REFERENCE), ("fast", MODE_FAST)):
+        sc = scenes.config1(seed=0, steps=steps)
+        sc.mode = mode
+        h = sc.dt / sc.sub_steps
+        # timed: every update back to back (the working set stays in L2)
+        s = sc.to_solver()
+        s.set_stream(stream.cuda_stream)
+        for _ in range(3):
+            s.update(sc.dt)
+        s.synchronize()
+        s.close()
+        s = sc.to_solver()
+        s.set_stream(stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                s.update(sc.dt)
+            e1.record(stream)
+        s.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        final_timed = s.read_state()
+        order = s.link_order() if mode == MODE_FAST else None
+        s.close()
+        # statistics: the same run again, state read back after every update
+        s = sc.to_solver()
+        e_start = energy(sc.pos, sc.prev, h, sc.gravity)
+        en, rmax, rp99 = [], [], []
+        for _ in range(steps):
+            s.update(sc.dt)
+            p, q = s.read_state()
+            en.append(energy(p, q, h, sc.gravity))
+            r = residual_of(p, sc)
+            rmax.append(float(r.max()))
+            rp99.append(float(np.percentile(r, 99)))
+        same_runs = bool(np.array_equal(p.view(np.uint32), final_timed[0].view(np.uint32)))
+        s.close()
+        # the CPU port of the reference over the same run (fast mode: the
+        # oracle replays the GPU's colour order)
+        o = load_scene(sc, link_order=order)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.update(sc.dt)
+        el = time.perf_counter() - t0
+        op, oq = o.particles()
+        units = sc.n_particles * sc.sub_steps * steps
+        en = np.asarray(en)
+        scale = max(abs(e_start), 1e-30)
+        out[name] = {
+            "gpu": {"value": units / (ms / 1e3), "ms_per_step": ms / steps},
+            "cpu": {"value": units / el, "ms_per_step": el / steps * 1e3, "cores": 1,
+                    "kind": "port"},
+            "bit_exact_vs_cpu_at_last_step": bool(
+                np.array_equal(p.view(np.uint32), op.view(np.uint32)) and
+                np.array_equal(q.view(np.uint32), oq.view(np.uint32))),
+            "timed_and_statistics_runs_identical": same_runs,
+            "residual": {"at_step": marks, "max": [rmax[k - 1] for k in marks],
+                         "p99": [rp99[k - 1] for k in marks]},
+            "energy": {"initial": e_start, "at_step": marks,
+                       "value": [float(en[k - 1]) for k in marks],
+                       "drift_rel_final": float((en[-1] - e_start) / scale),
+                       "max_abs_dev_rel": float(np.max(np.abs(en - e_start)) / scale)},
+        }
+    return out
+
+
 def run_config5(args, torch, flush, stream):
     """Configuration 5: 1024 cloth grids (1,048,576 particles, 3,999,744 links),
     20 sub-steps, 8 link iterations, particle collisions, 64 circles, 32
@@ -271,23 +376,112 @@ def run_config5(args, torch, flush, stream):
         torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
         v = sc.n_particles * sc.sub_steps / (ms / 1e3)
-        out[name] = {"value": v, "ms_per_step": ms,
-                     "residual_after": link_residual(s, sc),
-                     "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024,
-                     "roofline": step_roofline(v, step_bytes_per_unit(sc)),
-                     "kernel_rooflines": config5_kernel_rooflines(s, sc, torch, flush, stream)}
+        res = {"value": v, "ms_per_step": ms,
+               "residual_after": link_residual(s, sc),
+               "levels_per_sub_step_per_body": s.plan_stats()["levels"] / 1024,
+               "roofline": step_roofline(v, step_bytes_per_unit(sc)),
+               "kernel_rooflines": config5_kernel_rooflines(s, sc, torch, flush, stream)}
         s.close()
+        # statistics run: residual and energy after every update, and where
+        # the worst links are
+        s = sc.to_solver()
+        h = sc.dt / sc.sub_steps
+        e_start = energy(sc.pos, sc.prev, h, sc.gravity)
+        rmax, rp99, en = [], [], []
+        for _ in range(args.config5_steps):
+            s.update(sc.dt)
+            p, q = s.read_state()
+            r = residual_of(p, sc)
+            rmax.append(float(r.max()))
+            rp99.append(float(np.percentile(r, 99)))
+            en.append(energy(p, q, h, sc.gravity))
+        s.close()
+        inside, near_c = overlap_at_start(sc)
+        a, b = sc.la.astype(np.int64), sc.lb.astype(np.int64)
+        torn = r > 0.5
+        ends = np.concatenate([a[torn], b[torn]])
+        started = inside | near_c
+        res["per_step"] = {"residual_max": rmax, "residual_p99": rp99, "energy": en,
+                           "energy_initial": e_start,
+                           "energy_drift_rel_final": (en[-1] - e_start) / max(abs(e_start), 1e-30)}
+        torn_bodies = np.unique(ends // 1024)  # 1,024 particles per cloth body
+        res["stretched_links"] = {
+            "links_over_half_rest": int(torn.sum()),
+            "bodies_with_such_links": int(len(torn_bodies)),
+            "of_those_bodies_starting_with_a_particle_in_reach_of_a_polygon_or_circle": int(
+                len(np.intersect1d(torn_bodies, np.unique(np.nonzero(started)[0] // 1024)))),
+            "particles_starting_inside_or_within_reach_of_a_polygon": int(inside.sum()),
+            "particles_starting_within_reach_of_a_circle": int(near_c.sum())}
+        out[name] = res
+    return out
+
+
+def grid_buckets(sc) -> int:
+    """Collision-grid buckets of one world: a power of two >= 2 x particles, >= 64."""
+    n = max(2 * sc.n_particles, 64)
+    return 1 << (n - 1).bit_length()
+
+
+def kernel_byte_models(sc) -> dict:
+    """Algorithmic bytes per launch of every kernel of the sub-step pipeline,
+    each array counted once (f32 state, u32 indices).  name -> (bytes, model)."""
+    n, l, I = sc.n_particles, len(sc.la), sc.link_iters
+    nb = grid_buckets(sc)
+    nv = sum(len(g["points"]) for g in sc.polygons)
+    nc = len(sc.circles)
+    stiff = np.any(np.asarray(sc.stiff) != 1.0)
+    return {
+        "links": (I * l * ((16.0 if stiff else 12.0) + 32.0),
+                  "I x L x (12 B link record + 2 x (8 B read + 8 B write) of positions): "
+                  "logical bytes of the link passes; the executor keeps a body in shared "
+                  "memory through its passes, so DRAM sees only the body's load and store"),
+        "grid_count": (24.0 * n, "per particle: read pos 8 B, bucket counter atomic 8 B, "
+                                 "write (bucket, rank) 8 B"),
+        "grid_scan": (16.0 * nb, "per bucket: read count 4 B, clear it 4 B, write range 8 B"),
+        "grid_scatter": (40.0 * n, "per particle: read pos 8 B, (bucket, rank) 8 B, range 8 B, "
+                                   "write sorted entry 16 B"),
+        "collide_integrate": (56.0 * n + 8.0 * nb,
+                              "per particle: pos and prev read, pos and prev written (32 B), "
+                              "its sorted entry read (16 B), its (bucket, rank) slot 8 B; per "
+                              "bucket its range once (8 B); neighbour entries re-read through "
+                              "L1/L2 are not counted again"),
+        "rigid": (48.0 * (nc + nv), "per circle and polygon vertex: pos, prev, acc read and "
+                                    "written"),
+        "copy_back": (16.0 * n, "per particle: read pos from the second buffer, write it back"),
+    }
+
+
+def kernel_rooflines(prof: dict, sc, launches_per_step: dict) -> dict:
+    """Per-kernel rooflines of one update from the CUDA-event profile (each
+    launch timed alone, serially): achieved = algorithmic bytes per launch
+    (kernel_byte_models) / mean launch time, against the measured HBM copy
+    bandwidth.  The times of all kernels add up to the serial step time."""
+    peak, kind = _peaks()
+    models = kernel_byte_models(sc)
+    groups = {"links": [k for k in prof if k.startswith("exec_")],
+              "rigid": [k for k in prof if k.startswith("rigid")]}
+    for k in ("grid_count", "grid_scan", "grid_scatter", "collide_integrate", "copy_back"):
+        groups[k] = [k] if k in prof else []
+    out = {}
+    for g, names in groups.items():
+        ms = sum(prof[k] for k in names)
+        if ms <= 0.0:
+            continue
+        nl = launches_per_step.get(g, 1)
+        nbytes, model = models[g]
+        per_launch_ms = ms / nl
+        gbs = nbytes / (per_launch_ms / 1e3) / 1e9
+        out[g] = {"kernels": names, "ms_per_step": ms, "launches_per_step": nl,
+                  "algorithmic_bytes_per_launch": nbytes, "byte_model": model,
+                  "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                  "peak_source": kind}
+    out["serial_sum_ms_per_step"] = sum(prof.values())
     return out
 
 
 def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
-    """Per-kernel rooflines of one update at this throughput-bound size, from
-    the CUDA-event profile (each launch timed alone): the link executor
-    (every link pass of every sub-step: I x L x 44 B per sub-step) and
-    collide + bounds + integrate (32 B per particle per sub-step), against
-    the measured HBM copy bandwidth.  The link executor keeps each body in
-    shared memory through its passes, so its algorithmic bytes can exceed
-    what DRAM moves (ncu: ~41 MB read per launch)."""
+    """Per-kernel rooflines of one configuration-5 update at this
+    throughput-bound size (kernel_rooflines)."""
     with torch.cuda.stream(stream):
         flush.zero_()
     s.synchronize()
@@ -295,24 +489,37 @@ def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
     s.update(sc.dt)
     prof = s.profile()
     s.set_profiling(False)
-    peak, kind = _peaks()
-    n, l = sc.n_particles, len(sc.la)
-    groups = {
-        "links": ([k for k in prof if k.startswith("exec_")],
-                  sc.sub_steps * sc.link_iters * l * 44.0),
-        "collide_integrate": ([k for k in prof if k == "collide_integrate"],
-                              sc.sub_steps * 32.0 * n),
-    }
-    out = {}
-    for g, (names, nbytes) in groups.items():
-        ms = sum(prof[k] for k in names)
-        if ms <= 0.0:
-            continue
-        gbs = nbytes / (ms / 1e3) / 1e9
-        out[g] = {"kernels": names, "ms_per_step": ms, "algorithmic_bytes_per_step": nbytes,
-                  "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                  "peak_source": kind}
-    return out
+    S = sc.sub_steps
+    return kernel_rooflines(prof, sc, {"links": S, "grid_count": S, "grid_scan": S,
+                                       "grid_scatter": S, "collide_integrate": S,
+                                       "rigid": S + 1, "copy_back": 1})
+
+
+def overlap_at_start(sc):
+    """Solver particles that start inside a polygon (crossing number) or
+    within particle radius of a polygon edge, and those within reach of a
+    circle: the extension's one-way contacts push these out at the first
+    sub-step, by up to a polygon's depth."""
+    pos = sc.pos.astype(np.float64)
+    near_p = np.zeros(len(pos), bool)
+    for g in sc.polygons:
+        v = np.asarray(g["points"], np.float64)
+        ins = np.zeros(len(pos), bool)
+        for e in range(len(v)):
+            a, b = v[e], v[(e + 1) % len(v)]
+            cross = (a[1] > pos[:, 1]) != (b[1] > pos[:, 1])
+            dy = b[1] - a[1]
+            t = (pos[:, 1] - a[1]) / (dy if dy != 0.0 else 1.0)
+            ins ^= cross & (pos[:, 0] < a[0] + t * (b[0] - a[0]))
+            ab = b - a
+            u = np.clip(((pos - a) @ ab) / max(float(ab @ ab), 1e-30), 0.0, 1.0)
+            near_p |= np.linalg.norm(pos - (a + u[:, None] * ab), axis=1) < sc.radius
+        near_p |= ins
+    near_c = np.zeros(len(pos), bool)
+    for c in sc.circles:
+        near_c |= np.linalg.norm(pos - np.asarray(c["pos"], np.float64), axis=1) < \
+            float(c["radius"]) + sc.radius
+    return near_p, near_c
 
 
 def dist_env():
@@ -334,8 +541,18 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--serve-window", type=float, default=1.0)
+    ap.add_argument("--serve-window", type=float, default=10.0,
+                    help="arrival window of the stated 2,000 req/s rate (s)")
+    ap.add_argument("--serve-drain", type=float, default=150.0,
+                    help="longest wait for outstanding requests after a window (s)")
+    ap.add_argument("--serve-max-resident", type=int, default=2_000_000,
+                    help="residency limit of the server, solver particles (0: none)")
+    ap.add_argument("--serve-low-rate", type=float, default=150.0,
+                    help="arrival rate of the unsaturated serving run (req/s)")
+    ap.add_argument("--serve-low-window", type=float, default=30.0)
     ap.add_argument("--config5-steps", type=int, default=5)
+    ap.add_argument("--config1-steps", type=int, default=600)
+    ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-config5", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
@@ -345,10 +562,10 @@ def main():
         if rank != 0:
             return
         sc = build_scene()
-        warm = max(args.warmup, 0)
+        warm = max(args.warmup, 3)
         from oracle import load_scene
         o = load_scene(sc)
-        for _ in range(min(warm, 3)):
+        for _ in range(warm):
             o.update(sc.dt)
         # bounded sample: at most --steps updates, and at most ~cpu-budget seconds
         t0 = time.perf_counter()
@@ -362,10 +579,11 @@ def main():
         v = sc.n_particles * sc.sub_steps * k / el
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC,
-            "n_gpus": args.gpus, "steps": k, "warmup": min(warm, 3),
+            "n_gpus": args.gpus, "steps": k, "warmup": warm,
             "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "parallelism": "single-threaded reference"},
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator, bendy2d_gb300/scenes.py:config2)",
+            "config": config_dict(sc, world),
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": f"{k} updates of the full workload (C port of the "
                                        "reference, single thread like Solver::update)"},
@@ -457,9 +675,17 @@ def main():
     s.set_profiling(False)
     # launches of each kernel per step
     dom = max(prof_tot, key=prof_tot.get)
-    per_step_launches = {"exec_groups_links_smem": sc.sub_steps, "collide_integrate": sc.sub_steps,
-                         "grid_insert": sc.sub_steps, "rigid_ext": sc.sub_steps + 1}
-    nl = per_step_launches.get(dom, 1)
+
+    def launches_per_step(name: str) -> int:
+        if name.startswith("exec_") and "full" not in name:
+            return sc.sub_steps  # one link-phase launch per sub-step
+        if name in ("grid_count", "grid_scan", "grid_scatter", "collide_integrate"):
+            return sc.sub_steps
+        if name == "rigid_ext":
+            return sc.sub_steps + 1  # phase A of sub-step 0, B+A between sub-steps, B last
+        return 1
+
+    nl = launches_per_step(dom)
     dom_ms = prof_tot[dom] / nprof / nl
     peak, peak_kind = _peaks()
     alg = algorithmic_bytes(dom, sc)
@@ -491,29 +717,39 @@ def main():
     batched = None
     if not args.no_batched and world == 1:
         batched = run_batched_comparison(args, torch, flush, stream)
+    config1 = None
+    if not args.no_config1 and world == 1:
+        config1 = run_config1_long(args, torch, stream)
     config5 = None
     if not args.no_config5 and world == 1:
         config5 = run_config5(args, torch, flush, stream)
-    serving = None
+    serving = serving_low = None
     if not args.no_serve and world == 1:
-        from bendy2d_gb300.serving import run_poisson
+        from bendy2d_gb300.serving import request_pool, run_poisson
+        req_workload = ("worlds of log-uniform [64, 16384] particles built like configuration 2 "
+                        "(32-wide grids, particle collisions), steps uniform in [60, 600], "
+                        "dt 1/60, 8 sub-steps, 4 link iterations, 40 GB budget")
+        pool = request_pool(64, 0)
+        # the stated rate offers ~15.5 G particle-substeps/s, several times what
+        # one GPU serves: a bounded window measures the served capacity, and
+        # its latencies measure the backlog
         serving = run_poisson(lam=2000.0, duration=args.serve_window, seed=0,
-                              budget_bytes=40 << 30, pool=64, drain_s=120.0)
-        serving["workload"] = ("Poisson arrivals at 2000 req/s for the window, worlds of "
-                               "log-uniform [64, 16384] particles built like configuration 2 "
-                               "(grids, particle collisions), steps uniform in [60, 600], "
-                               "dt 1/60, 8 sub-steps, 40 GB budget")
+                              budget_bytes=40 << 30, drain_s=args.serve_drain,
+                              scenes_pool=pool, max_resident_particles=args.serve_max_resident)
+        serving["workload"] = "Poisson arrivals at 2000 req/s, " + req_workload
+        # an arrival rate below the served capacity: latencies measure service
+        serving_low = run_poisson(lam=args.serve_low_rate, duration=args.serve_low_window,
+                                  seed=1, budget_bytes=40 << 30, drain_s=args.serve_drain,
+                                  scenes_pool=pool, max_resident_particles=args.serve_max_resident)
+        serving_low["workload"] = (f"Poisson arrivals at {args.serve_low_rate:g} req/s, "
+                                   + req_workload)
 
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generator, bendy2d_gb300/scenes.py:config2)",
-        "config": {"workload": WORKLOAD, "particles": sc.n_particles, "links": int(len(sc.la)),
-                   "sub_steps": sc.sub_steps, "link_iters": sc.link_iters,
-                   "mode": "reference-order", "collisions": "pp+pc+ppoly",
-                   "l2": "flushed (256 MiB write) between timed steps",
-                   "parallelism": f"replicas x{world}"},
+        "config": config_dict(sc, world),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
@@ -521,12 +757,19 @@ def main():
                      "traffic": traffic, "algorithmic_bytes_per_launch": alg,
                      "launch_ms": dom_ms, "chain": chain},
         "kernel_ms_per_step": {k: v / nprof for k, v in sorted(prof_tot.items())},
+        "kernel_rooflines": kernel_rooflines(
+            {k: v / nprof for k, v in prof_tot.items()}, sc,
+            {"links": sc.sub_steps, "grid_count": sc.sub_steps, "grid_scan": sc.sub_steps,
+             "grid_scatter": sc.sub_steps, "collide_integrate": sc.sub_steps,
+             "rigid": sc.sub_steps + 1, "copy_back": 1}),
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "batched_config3": batched,
         "serving_config4": serving,
+        "serving_unsaturated": serving_low,
         "stress_config5": config5,
+        "long_run_config1": config1,
     }
     print(json.dumps(out))
     if world > 1:

@@ -7,10 +7,8 @@ through the C ABI in include/bendy2d.h; there is no CPU fallback.
 """
 from .api import (COLLIDE_PC, COLLIDE_PP, COLLIDE_PPOLY, MODE_FAST, MODE_REFERENCE, B2DError,
                   Batch, Bounds, Circle, CircleLink, Link, Particle, ParticleLink, Polygon,
-                  Solver, line_intersection, proj_a_on_b, proj_a_on_b_clamped,
-                  proj_point_on_line)
+                  Solver, line_intersection)
 
 __all__ = ["Solver", "Particle", "Link", "ParticleLink", "CircleLink", "Circle", "Polygon",
            "Bounds", "Batch", "B2DError", "MODE_REFERENCE", "MODE_FAST", "COLLIDE_PP",
-           "COLLIDE_PC", "COLLIDE_PPOLY", "line_intersection", "proj_a_on_b",
-           "proj_a_on_b_clamped", "proj_point_on_line"]
+           "COLLIDE_PC", "COLLIDE_PPOLY", "line_intersection"]

@@ -11,6 +11,7 @@ from pathlib import Path
 _LIB_PATH = Path(__file__).resolve().parent / "_build" / "libbendy2d_gb300.so"
 
 B2D_OK = 0
+FAULT_WAIT_TIMEOUT, FAULT_GRID_CAP, FAULT_ALLOC = 1, 2, 3
 ERRORS = {
     1: "null argument", 2: "particle link index", 3: "circle link index",
     4: "polygon link index", 5: "bad argument", 6: "index out of range", 7: "CUDA error",
@@ -53,7 +54,7 @@ class CServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "admitted", "completed", "failed",
                                           "queued", "active", "ticks", "particle_substeps",
                                           "resident_bytes", "admit_ns", "step_ns",
-                                          "retire_ns")]
+                                          "retire_ns", "cancelled", "resident_particles")]
 
 
 class CPlanStats(C.Structure):
@@ -98,6 +99,7 @@ SIGNATURES = {
     "b2d_set_circle_static": [_P, C.c_size_t, C.c_int],
     "b2d_set_tuning": [_P, C.c_char_p, C.c_double],
     "b2d_update": [_P, C.c_float],
+    "b2d_set_fault": [_P, C.c_int, C.c_uint64],
     "b2d_get_particle_len": [_P, _SZ],
     "b2d_get_circles_len": [_P, _SZ],
     "b2d_get_polygons_len": [_P, _SZ],
@@ -145,6 +147,9 @@ SIGNATURES = {
     "b2d_server_stop": [_P],
     "b2d_server_submit": [_P, _P, C.c_uint32, C.c_float, C.POINTER(C.c_uint64)],
     "b2d_server_poll": [_P, C.c_uint64, C.POINTER(C.c_int)],
+    "b2d_server_cancel": [_P, C.c_uint64],
+    "b2d_server_set_max_resident_particles": [_P, C.c_uint64],
+    "b2d_server_set_fault": [_P, C.c_int, C.c_uint64],
     "b2d_server_take": [_P, C.c_uint64, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "b2d_server_get_stats": [_P, C.POINTER(CServerStats)],
     "b2d_server_finished": [_P, C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_size_t)],

@@ -329,34 +329,6 @@ def line_intersection(line1, line2):
     return None
 
 
-def proj_a_on_b(a, b):
-    """common::proj_a_on_b, src/common.rs:28-32: a.dot(b) / |b|^2 * b."""
-    (ax, ay), (bx, by) = _f2(a), _f2(b)
-    k = (ax * bx + ay * by) / (bx * bx + by * by)
-    return _py((k * bx, k * by))
-
-
-def proj_a_on_b_clamped(a, b):
-    """common::proj_a_on_b_clamped, src/common.rs:34-44: the projection,
-    replaced by b when it is greater than b in every component and by zero
-    when it is less than zero in every component (nalgebra's component-wise
-    vector comparison)."""
-    p = _f2(proj_a_on_b(a, b))
-    bb = _f2(b)
-    if p[0] > bb[0] and p[1] > bb[1]:
-        return _py(bb)
-    if p[0] < 0 and p[1] < 0:
-        return (0.0, 0.0)
-    return _py(p)
-
-
-def proj_point_on_line(point, line):
-    """common::proj_point_on_line, src/common.rs:46-52."""
-    (sx, sy), (ex, ey), (px, py) = _f2(line[0]), _f2(line[1]), _f2(point)
-    q = _f2(proj_a_on_b_clamped((px - sx, py - sy), (ex - sx, ey - sy)))
-    return _py((sx + q[0], sy + q[1]))
-
-
 def _cpart(p: Particle) -> N.CParticle:
     return N.CParticle(N.Vec2(*p.pos), N.Vec2(*p.prev_pos), N.Vec2(*p.acc))
 
@@ -521,6 +493,11 @@ class Solver:
         """Executor tunables (see include/bendy2d.h b2d_set_tuning)."""
         for k, v in kv.items():
             self._chk(self._lib.b2d_set_tuning(self._h, k.encode(), float(v)))
+
+    def set_fault(self, kind: int, value: int) -> None:
+        """Fault injection for tests of failure detection (FAULT_* of
+        _native; value 0 turns it off)."""
+        self._chk(self._lib.b2d_set_fault(self._h, int(kind), int(value)))
 
     # ---- update (src/solver.rs:106-116)
     def update(self, dt: float) -> None:

@@ -127,8 +127,13 @@ struct DScheds {
   const uint32_t* chunk_len;  // words (multiple of 4)
   const uint32_t* stream;
   uint32_t* err;
+  uint32_t fault;  // FAULT_BIT_* test switches (0 in normal operation)
 };
 enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_GRID_OVERFLOW = 2u };
+// Test switch for failure detection: every executor group treats its first
+// bulk-copy wait as timed out (and takes the timeout path: error word, wait
+// for the copy in flight to land, leave) without a real timeout.
+enum : uint32_t { FAULT_BIT_WAIT = 1u };
 
 // Extension broadphase: hashed uniform grid built by a counting sort each
 // sub-step.  Every world with particle collisions owns a power-of-two range

@@ -362,6 +362,16 @@ int b2d_set_tuning(b2d_solver* s, const char* key, double value) {
   return OK;
 }
 
+int b2d_set_fault(b2d_solver* s, int kind, uint64_t value) {
+  CHECK_S(s);
+  if (s->batch) return fail(ERR_STATE, "solver belongs to a batch");
+  Engine* e = nullptr;
+  int st = engine_for(s, &e);
+  if (st != OK) return st;
+  st = e->set_fault(kind, value);
+  return st == OK ? OK : fail(st, e->last_error);
+}
+
 int b2d_update(b2d_solver* s, float dt) {
   CHECK_S(s);
   if (s->batch) return fail(ERR_STATE, "solver belongs to a batch: use b2d_batch_update");
@@ -766,6 +776,25 @@ int b2d_server_submit(b2d_server* sv, b2d_solver* world, uint32_t steps, float d
   st = sv->sv->submit(world->w, steps, dt, id, &why);
   return st == OK ? OK : fail(st, why);
 }
+int b2d_server_cancel(b2d_server* sv, uint64_t id) {
+  if (!sv) return fail(ERR_NULL, "null server");
+  const int st = sv->sv->cancel(id);
+  if (st == ERR_INDEX) return fail(st, "unknown request id");
+  if (st == ERR_STATE) return fail(st, "request already finished");
+  return st;
+}
+int b2d_server_set_max_resident_particles(b2d_server* sv, uint64_t n) {
+  if (!sv) return fail(ERR_NULL, "null server");
+  sv->sv->set_max_resident_particles(n);
+  return OK;
+}
+int b2d_server_set_fault(b2d_server* sv, int kind, uint64_t value) {
+  if (!sv) return fail(ERR_NULL, "null server");
+  if (kind != FAULT_WAIT_TIMEOUT && kind != FAULT_GRID_CAP && kind != FAULT_ALLOC)
+    return fail(ERR_ARG, "unknown fault kind " + std::to_string(kind));
+  sv->sv->set_fault(kind, value);
+  return OK;
+}
 int b2d_server_poll(b2d_server* sv, uint64_t id, int* state) {
   if (!sv || !state) return fail(ERR_NULL, "null argument");
   int st = sv->sv->poll(id, state);
@@ -809,6 +838,8 @@ int b2d_server_get_stats(b2d_server* sv, b2d_server_stats* out) {
   out->admit_ns = s.admit_ns;
   out->step_ns = s.step_ns;
   out->retire_ns = s.retire_ns;
+  out->cancelled = s.cancelled;
+  out->resident_particles = s.resident_particles;
   return OK;
 }
 

@@ -45,10 +45,10 @@ static constexpr uint32_t kSerialPackThreads = 64;       // bodies per serial pa
 
 // Kernel launch; pdl: programmatic dependent launch — the kernel may start
 // while the previous kernel in the stream finishes (it calls pdl_wait()
-// before touching that kernel's results).
+// before touching that kernel's results).  Returns the launch's own status.
 template <typename... P, typename... A>
-static void launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                     bool pdl, A... args) {
+static cudaError_t launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                            bool pdl, A... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -59,7 +59,7 @@ static void launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaSt
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1u : 0u;
-  cudaLaunchKernelEx(&cfg, k, args...);
+  return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
 Engine::Engine(cudaStream_t stream) : stream_(stream) {
@@ -213,7 +213,45 @@ int Engine::plan(const WorldHost& w, WorldImage* img, std::string* why) {
   return plan_world(w, tune_, reg_, *img, why);
 }
 
+int Engine::set_fault(int kind, uint64_t value) {
+  switch (kind) {
+    case FAULT_WAIT_TIMEOUT:
+      fault_bits_ = value ? (fault_bits_ | FAULT_BIT_WAIT) : (fault_bits_ & ~FAULT_BIT_WAIT);
+      break;
+    case FAULT_GRID_CAP:
+      fault_grid_cap_ = (uint32_t)std::min<uint64_t>(value, 0xFFFFFFFFu);
+      break;
+    case FAULT_ALLOC:
+      fault_alloc_ = value;
+      return OK;  // host side only: the launch sequence is unchanged
+    default:
+      last_error = "unknown fault kind " + std::to_string(kind);
+      return ERR_ARG;
+  }
+  invalidate_graph();  // the kernels' parameters change
+  return OK;
+}
+
+// The world block is allocated and uploaded before a slot is taken, so a
+// failed allocation or copy leaves the engine as it was.
 int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
+  const BlockLayout L = layout_of(img);
+  unsigned char* block = nullptr;
+  if (fault_alloc_ > 0) {
+    --fault_alloc_;
+    last_error = "cudaMallocAsync: injected allocation failure";
+    return ERR_CUDA;
+  }
+  B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&block), L.total, stream_));
+  std::vector<unsigned char> stage(L.total);
+  write_block(img, L, stage.data());
+  cudaError_t ce = cudaMemcpyAsync(block, stage.data(), L.total, cudaMemcpyHostToDevice, stream_);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);  // the staging buffer is pageable
+  if (ce != cudaSuccess) {
+    last_error = std::string("uploading a world block: ") + cudaGetErrorString(ce);
+    cudaFreeAsync(block, stream_);
+    return ERR_CUDA;
+  }
   uint32_t slot;
   if (!free_slots_.empty()) {
     slot = free_slots_.back();
@@ -225,17 +263,16 @@ int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
   Slot& s = slots_[slot];
   s.img = std::move(img);
   s.host = w;
-  s.L = layout_of(s.img);
-  B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&s.block), s.L.total, stream_));
-  dev_bytes_ += s.L.total;
-  std::vector<unsigned char> stage(s.L.total);
-  write_block(s.img, s.L, stage.data());
-  B2D_CUDA(cudaMemcpyAsync(s.block, stage.data(), s.L.total, cudaMemcpyHostToDevice, stream_));
+  s.L = L;
+  s.block = block;
   s.live = true;
-  const int st = fill_world_record(slot);
-  if (st != OK) return st;
-  B2D_CUDA(cudaStreamSynchronize(stream_));  // the staging buffer is pageable
+  dev_bytes_ += L.total;
   lists_dirty_ = true;
+  const int st = fill_world_record(slot);
+  if (st != OK) {
+    remove(slot);
+    return st;
+  }
   *out_slot = slot;
   return OK;
 }
@@ -666,6 +703,12 @@ int Engine::rebuild_lists() {
 int Engine::launch_all(bool profiling) {
   launches_ = 0;
   prof_.clear();
+  // the first failed launch of this step (launch_k reports each launch's own
+  // status; the <<<>>> launches are covered by cudaGetLastError at the end)
+  cudaError_t launch_err = cudaSuccess;
+  auto lk = [&](cudaError_t e) {
+    if (e != cudaSuccess && launch_err == cudaSuccess) launch_err = e;
+  };
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (profiling) {
     cudaEventCreate(&e0);
@@ -686,8 +729,10 @@ int Engine::launch_all(bool profiling) {
       if (!found) prof_.emplace_back(name, ms);
     }
   };
-  const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_};
+  const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_, fault_bits_};
   grid_.err = d_err_;
+  DGrid GR = grid_;  // as launched: the capacity may be lowered by FAULT_GRID_CAP
+  if (fault_grid_cap_ && fault_grid_cap_ < GR.cap) GR.cap = fault_grid_cap_;
   const DWorld* W = d_worlds_;
   // Streams: link executors, grid and collide kernels run on the main
   // stream; circle/polygon kernels on aux streams (graph branches), joined
@@ -751,7 +796,7 @@ int Engine::launch_all(bool profiling) {
         c.res ? (c.full ? k_exec_groups<true, true, true> : k_exec_groups<false, true, true>)
         : c.full ? (c.smem ? k_exec_groups<true, true, false> : k_exec_groups<true, false, false>)
                  : (c.smem ? k_exec_groups<false, true, false> : k_exec_groups<false, false, false>);
-    launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub);
+    lk(launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub));
   };
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
@@ -868,27 +913,27 @@ int Engine::launch_all(bool profiling) {
       const uint32_t tile = small ? SCAN_SMALL_TILE : SCAN_LARGE_TILE;
       const uint32_t nt = (grid_used_ + tile - 1) / tile;
       timed("grid_count", [&] {
-        launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH, nch,
-                 cur, s);
+        lk(launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GR, CH,
+                    nch, cur, s));
       });
       const uint32_t ncta = small ? nt : std::min<uint32_t>(nt, (uint32_t)std::max(g_num_sms, 1));
       timed("grid_scan", [&] {
         if (small)
-          launch_k(k_grid_scan<1, 256>, dim3(ncta), dim3(256), 0, stream_, !profiling, grid_,
-                   grid_used_, nt);
+          lk(launch_k(k_grid_scan<1, 256>, dim3(ncta), dim3(256), 0, stream_, !profiling, GR,
+                      grid_used_, nt));
         else
-          launch_k(k_grid_scan<4, 1024>, dim3(ncta), dim3(1024), 0, stream_, !profiling, grid_,
-                   grid_used_, nt);
+          lk(launch_k(k_grid_scan<4, 1024>, dim3(ncta), dim3(1024), 0, stream_, !profiling, GR,
+                      grid_used_, nt));
       });
       timed("grid_scatter", [&] {
-        launch_k(k_grid_scatter, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, grid_, CH,
-                 nch, cur, s);
+        lk(launch_k(k_grid_scatter, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GR, CH,
+                    nch, cur, s));
       });
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0, stream_,
-               !profiling, W, grid_, CH, nch, cur, s);
+      lk(launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0,
+                  stream_, !profiling, W, GR, CH, nch, cur, s));
     });
     if (nre) edge(stream_, ax);
   }
@@ -901,6 +946,11 @@ int Engine::launch_all(bool profiling) {
   if (profiling) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+  }
+  if (launch_err != cudaSuccess) {
+    last_error = std::string("cudaLaunchKernelEx: ") + cudaGetErrorString(launch_err);
+    cudaGetLastError();  // the same failure, recorded by the runtime too
+    return ERR_CUDA;
   }
   B2D_CUDA(cudaGetLastError());
   return OK;

@@ -16,6 +16,17 @@ typedef struct CUgraphExec_st* cudaGraphExec_t;
 
 namespace b2d {
 
+// Fault injection for tests of failure handling (b2d_set_fault): the kinds.
+//  FAULT_WAIT_TIMEOUT  value != 0: every executor group's first bulk-copy wait
+//                      reports a timeout (the copy still lands before the CTA
+//                      leaves); the step then reports ERR_DEVICE
+//  FAULT_GRID_CAP      value > 0: the collision grid hands out at most `value`
+//                      sorted entries per sub-step (below the particle count
+//                      this makes the scan refuse blocks: ERR_BIT_GRID_OVERFLOW)
+//  FAULT_ALLOC         the next `value` world-block allocations fail as if
+//                      cudaMallocAsync had failed
+enum : int { FAULT_WAIT_TIMEOUT = 1, FAULT_GRID_CAP = 2, FAULT_ALLOC = 3 };
+
 // Tunables of the planner (the autotuner sweeps these).
 struct PlanTuning {
   float serial_width = 2.0f;        // single-pass width below which a body runs serially
@@ -146,6 +157,7 @@ class Engine {
   PlanTuning& tuning() { return tune_; }
   void set_tuning(const PlanTuning& t);
   size_t device_bytes() const { return dev_bytes_; }
+  int set_fault(int kind, uint64_t value);  // FAULT_*; ERR_ARG for an unknown kind
   std::string last_error;
 
  private:
@@ -240,6 +252,10 @@ class Engine {
   std::vector<std::pair<std::string, float>> prof_;
   uint32_t launches_ = 0;
   size_t dev_bytes_ = 0;
+  // fault injection (tests only; all zero in normal operation)
+  uint32_t fault_bits_ = 0;       // FAULT_BIT_* for the kernels
+  uint32_t fault_grid_cap_ = 0;   // 0: the grid's real capacity
+  uint64_t fault_alloc_ = 0;      // world-block allocations still to fail
 };
 
 }  // namespace b2d

@@ -8,19 +8,25 @@
 // the device and stall the frame), and hosts that hand this library device
 // buffers they own and manage themselves.
 //
-// The scratch array (NOALLOC_BYTES, about 3.6 MB) stays resident on every GPU
-// that loads the library until the process exits.  Every call shares it and
-// it keeps the previous call's contents, so each call clears what must start
-// at zero; calls whose GPU work overlaps (different streams, or host threads
-// racing) corrupt each other.  The scan's cursor lives there too (the count
-// pass resets it every sub-step); a range past the scratch entries would be
-// refused and recorded as ERR_BIT_GRID_OVERFLOW in a scratch word (O_ERR)
-// that a debugger can read, since this asynchronous call returns before the
-// GPU work runs.
+// The scratch array (NOALLOC_BYTES, about 3.6 MB) is part of the library's
+// device image: a GPU maps it when the library's kernels are first loaded on
+// it (with lazy module loading, at the first call on that device) and holds it
+// until the process exits.  Every call shares it and it keeps the previous
+// call's contents, so each call clears what must start at zero; calls whose
+// GPU work overlaps (different streams, or host threads racing) corrupt each
+// other.  The scan's cursor lives there too (the count pass resets it every
+// sub-step); a range past the scratch entries would be refused and recorded
+// as ERR_BIT_GRID_OVERFLOW in a scratch word (O_ERR) that a debugger can
+// read, since this asynchronous call returns before the GPU work runs.
 //
-// First call on a device: it resolves the array's device address with
-// cudaGetSymbolAddress while that device is current.  Make that first call
-// before capturing a CUDA stream into a graph.
+// The array's device address: host code cannot use the array's name (that is
+// a host-side stand-in), so every call outside stream capture looks the
+// address up with cudaGetSymbolAddress on the current device, which also
+// stays right after a cudaDeviceReset gave the device a new context.  A call
+// made while its stream is being captured reuses the address that the last
+// call outside capture found on that device, because the lookup may load the
+// module, which capture does not allow: make the first call on each device
+// before capturing.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -55,7 +61,8 @@ constexpr size_t NOALLOC_BYTES = O_POS1 + up256(8 * NOALLOC_MAX_PARTICLES);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-// device address of g_noalloc_scratch per device ordinal, resolved once
+// device address of g_noalloc_scratch per device ordinal, as found by the
+// last call outside stream capture
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char* g_addr[kMaxDevices] = {};
@@ -63,6 +70,17 @@ unsigned char* g_addr[kMaxDevices] = {};
 int fail(int code, const std::string& m) {
   set_last_error(m);
   return code;
+}
+
+// one launch; returns its own status (an error left by earlier, unrelated
+// work on this thread is neither reported nor cleared)
+template <typename... P, typename... A>
+cudaError_t launch(void (*k)(P...), uint32_t grid, uint32_t block, cudaStream_t st, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = st;
+  return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
 // Writes the world record and the chunk list into the scratch array; the
@@ -93,19 +111,25 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(B2D_ERR_CUDA, "no current CUDA device");
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess)
+    return fail(B2D_ERR_CUDA, "cudaStreamIsCapturing failed on the given stream");
   unsigned char* base;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
       void* a = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
       if (e != cudaSuccess || !a)
         return fail(B2D_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_addr[dev] = static_cast<unsigned char*>(a);
+    } else if (!g_addr[dev]) {
+      return fail(B2D_ERR_STATE, "the first b2d_collide_substeps_noalloc call on a device must "
+                                 "come before stream capture");
     }
     base = g_addr[dev];
   }
-  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
   const uint32_t np = (uint32_t)n;
   uint32_t nb = 64;
   while (nb < 2 * np) nb <<= 1;
@@ -147,20 +171,32 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   G.nbuckets = nb;
   G.cap = np;
 
-  k_noalloc_setup<<<(nch + 255) / 256, 256, 0, st>>>(w, chunks, nch, dW);
+  auto bad = [](cudaError_t e, const char* what) {
+    return fail(B2D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  cudaError_t e = launch(k_noalloc_setup, (nch + 255) / 256, 256, st, w, chunks, nch, dW);
+  if (e != cudaSuccess) return bad(e, "setup launch");
   // bucket counts start from zero (each scan clears what it read; this also
   // covers a call that stopped part-way)
-  if (cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st) != cudaSuccess)
-    return fail(B2D_ERR_CUDA, "clearing the bucket counts failed");
+  if ((e = cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st)) != cudaSuccess)
+    return bad(e, "clearing the bucket counts");
   for (uint32_t s = 0; s < w.S; ++s) {
     const uint32_t cur = s & 1u;
-    k_grid_count<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_grid_scan<1, 256><<<nt, 256, 0, st>>>(G, nb, nt);  // nb <= 131072: small tiles
-    k_grid_scatter<<<nch, CHUNK, 0, st>>>(dW, G, chunks, nch, cur, s);
-    k_collide_integrate<<<nch * COLLIDE_CTAS, COLLIDE_THREADS, 0, st>>>(dW, G, chunks, nch, cur, s);
+    if ((e = launch(k_grid_count, nch, CHUNK, st, (const DWorld*)dW, G, (const uint2*)chunks, nch,
+                    cur, s)) != cudaSuccess)
+      return bad(e, "count launch");
+    // nb <= 131072: small tiles
+    if ((e = launch(k_grid_scan<1, 256>, nt, 256, st, G, nb, nt)) != cudaSuccess)
+      return bad(e, "scan launch");
+    if ((e = launch(k_grid_scatter, nch, CHUNK, st, (const DWorld*)dW, G, (const uint2*)chunks,
+                    nch, cur, s)) != cudaSuccess)
+      return bad(e, "scatter launch");
+    if ((e = launch(k_collide_integrate, nch * COLLIDE_CTAS, COLLIDE_THREADS, st,
+                    (const DWorld*)dW, G, (const uint2*)chunks, nch, cur, s)) != cudaSuccess)
+      return bad(e, "collide launch");
   }
-  k_copy_back<<<nch, CHUNK, 0, st>>>(dW, chunks, nch);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(B2D_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  if ((e = launch(k_copy_back, nch, CHUNK, st, (const DWorld*)dW, (const uint2*)chunks, nch)) !=
+      cudaSuccess)
+    return bad(e, "copy-back launch");
   return B2D_OK;
 }

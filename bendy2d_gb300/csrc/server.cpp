@@ -16,6 +16,10 @@
 // stays device-resident across ticks.  Every world is computed independently
 // (per-world grids, order-independent sums), so a result is bit-identical
 // whether the request ran alone or in a mix.
+//
+// Cancellation: a queued request is dropped at once; one taken for planning
+// or resident on the device is dropped by the worker at its next install or
+// retire phase, so no kernel of the tick in flight loses its world.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -38,8 +42,10 @@ struct Server::Req {
   uint32_t steps = 0, done = 0;
   float dt = 0.0f;
   int state = SERVE_QUEUED;
+  bool cancel = false;  // cancellation asked after the worker took it
   uint32_t slot = 0;
   size_t bytes = 0;
+  uint64_t np = 0;      // solver particles (the residency limit counts these)
   Clock::time_point t_submit, t_admit, t_done;
   std::string error;
 };
@@ -99,6 +105,7 @@ int Server::submit(const WorldHost& w, uint32_t steps, float dt, uint64_t* id, s
   r->steps = steps;
   r->dt = dt;
   r->bytes = bytes;
+  r->np = w.particles.size();
   r->t_submit = Clock::now();
   {
     std::lock_guard<std::mutex> lk(mu_);
@@ -120,14 +127,46 @@ int Server::poll(uint64_t id, int* state) {
   return OK;
 }
 
+int Server::cancel(uint64_t id) {
+  std::lock_guard<std::mutex> lk(mu_);
+  auto it = reqs_.find(id);
+  if (it == reqs_.end()) return ERR_INDEX;
+  Req& r = *it->second;
+  if (r.state != SERVE_QUEUED && r.state != SERVE_RUNNING) return ERR_STATE;
+  auto q = std::find(queue_.begin(), queue_.end(), &r);
+  if (q != queue_.end()) {  // not yet taken by the worker
+    queue_.erase(q);
+    r.state = SERVE_CANCELLED;
+    r.t_admit = r.t_done = Clock::now();
+    ++stats_.cancelled;
+    finished_.push_back(r.id);
+    return OK;
+  }
+  r.cancel = true;  // the worker drops it at its next install or retire
+  return OK;
+}
+
+void Server::set_max_resident_particles(uint64_t n) {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    max_resident_np_ = n;
+  }
+  cv_.notify_all();
+}
+
+void Server::set_fault(int kind, uint64_t value) {
+  std::lock_guard<std::mutex> lk(mu_);
+  faults_.emplace_back(kind, value);
+}
+
 int Server::take(uint64_t id, WorldHost* out, double* latency_s, double* queue_s,
                  std::string* why) {
   std::lock_guard<std::mutex> lk(mu_);
   auto it = reqs_.find(id);
   if (it == reqs_.end()) return ERR_INDEX;
   Req& r = *it->second;
-  if (r.state == SERVE_FAILED) {
-    if (why) *why = r.error;
+  if (r.state == SERVE_FAILED || r.state == SERVE_CANCELLED) {
+    if (why) *why = r.state == SERVE_CANCELLED ? std::string("request cancelled") : r.error;
     reqs_.erase(it);
     return ERR_STATE;
   }
@@ -155,6 +194,7 @@ ServerStats Server::stats() {
   s.queued = queue_.size();
   s.active = active_.size();
   s.resident_bytes = resident_;
+  s.resident_particles = resident_np_;
   return s;
 }
 
@@ -163,15 +203,19 @@ void Server::loop() {
   // requests taken from the queue and planned during the last tick, waiting
   // to be installed after it
   std::vector<std::pair<Req*, WorldImage>> planned;
-  auto fail = [&](Req* r, const std::string& why) {
+  // a request taken from the queue leaves before it reached the device:
+  // failed (planning or install) or cancelled
+  auto drop = [&](Req* r, int state, const std::string& why) {
     std::lock_guard<std::mutex> lk(mu_);
-    r->t_admit = Clock::now();
-    r->state = SERVE_FAILED;
+    r->t_admit = r->t_done = Clock::now();
+    r->state = state;
     r->error = why;
     resident_ -= r->bytes;
-    ++stats_.failed;
+    resident_np_ -= r->np;
+    ++(state == SERVE_CANCELLED ? stats_.cancelled : stats_.failed);
     finished_.push_back(r->id);
   };
+  auto fail = [&](Req* r, const std::string& why) { drop(r, SERVE_FAILED, why); };
   auto plan = [&](Req* r) {
     WorldImage img;
     std::string why;
@@ -181,21 +225,28 @@ void Server::loop() {
   };
   for (;;) {
     std::vector<Req*> taken;
+    std::vector<std::pair<int, uint64_t>> faults;
     {
       std::unique_lock<std::mutex> lk(mu_);
       cv_.wait(lk, [&] {
         return !running_ || !queue_.empty() || !active_.empty() || !planned.empty();
       });
       if (!running_) break;
-      // first come, first served while the budget holds
-      while (!queue_.empty() && resident_ + queue_.front()->bytes <= budget_) {
+      // first come, first served while the memory budget and the residency
+      // limit hold (one request is always taken onto an idle device)
+      while (!queue_.empty() && resident_ + queue_.front()->bytes <= budget_ &&
+             (max_resident_np_ == 0 || resident_np_ == 0 ||
+              resident_np_ + queue_.front()->np <= max_resident_np_)) {
         Req* r = queue_.front();
         queue_.pop_front();
         resident_ += r->bytes;
+        resident_np_ += r->np;
         taken.push_back(r);
       }
+      faults.swap(faults_);
     }
     if (!eng) eng = std::make_unique<Engine>(nullptr);
+    for (const auto& f : faults) eng->set_fault(f.first, f.second);
     const Clock::time_point ta = Clock::now();
     // with nothing on the device there is no tick to plan under: plan now
     bool idle;
@@ -209,6 +260,15 @@ void Server::loop() {
     }
     for (auto& pr : planned) {
       Req* r = pr.first;
+      bool cancelled;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        cancelled = r->cancel;
+      }
+      if (cancelled) {
+        drop(r, SERVE_CANCELLED, "request cancelled");
+        continue;
+      }
       uint32_t slot = 0;
       int st = eng->add_planned(&r->world, std::move(pr.second), &slot);
       if (st == OK) st = eng->set_dt(slot, r->dt);
@@ -248,23 +308,35 @@ void Server::loop() {
     const Clock::time_point tr = Clock::now();
     uint64_t units = 0;
     std::vector<Req*> finished;
-    for (Req* r : act) {
+    std::vector<char> cancelled;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      for (Req* r : act) cancelled.push_back(r->cancel ? 1 : 0);
+    }
+    for (size_t k = 0; k < act.size(); ++k) {
+      Req* r = act[k];
       if (r->done < r->steps) {
         ++r->done;
         units += (uint64_t)r->world.particles.size() * r->world.sub_steps;
       }
-      if (r->done >= r->steps || st != OK) finished.push_back(r);
+      if (r->done >= r->steps || st != OK || cancelled[k]) finished.push_back(r);
     }
     for (Req* r : finished) {
-      int ds = st == OK ? eng->download(r->slot) : st;
+      const bool cancel_it = cancelled[std::find(act.begin(), act.end(), r) - act.begin()] != 0;
+      int ds = st != OK ? st : (cancel_it ? OK : eng->download(r->slot));
+      const std::string err = ds != OK ? eng->last_error : std::string();
       eng->remove(r->slot);
       std::lock_guard<std::mutex> lk(mu_);
       r->t_done = Clock::now();
       resident_ -= r->bytes;
+      resident_np_ -= r->np;
       if (ds != OK) {
         r->state = SERVE_FAILED;
-        r->error = eng->last_error;
+        r->error = err;
         ++stats_.failed;
+      } else if (cancel_it) {
+        r->state = SERVE_CANCELLED;
+        ++stats_.cancelled;
       } else {
         r->state = SERVE_DONE;
         ++stats_.completed;

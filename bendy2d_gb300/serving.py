@@ -19,7 +19,7 @@ import numpy as np
 from . import _native as N
 from .api import Solver
 
-QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+QUEUED, RUNNING, DONE, FAILED, CANCELLED = 0, 1, 2, 3, 4
 
 
 class Server:
@@ -56,6 +56,21 @@ class Server:
         N.check(self._lib.b2d_server_poll(self._h, rid, C.byref(st)))
         return st.value
 
+    def cancel(self, rid: int) -> None:
+        """Drop a request: a queued one at once, a running one when the tick
+        in flight ends; it is then listed by finished() as CANCELLED."""
+        N.check(self._lib.b2d_server_cancel(self._h, rid))
+
+    def set_max_resident_particles(self, n: int) -> None:
+        """Admission keeps the resident solver particles at or below n (0: no
+        limit); one request is always admitted onto an idle device."""
+        N.check(self._lib.b2d_server_set_max_resident_particles(self._h, int(n)))
+
+    def set_fault(self, kind: int, value: int) -> None:
+        """Fault injection for tests (FAULT_* of _native), applied before the
+        worker's next tick."""
+        N.check(self._lib.b2d_server_set_fault(self._h, int(kind), int(value)))
+
     def finished(self, cap: int = 4096) -> list:
         buf = (C.c_uint64 * cap)()
         n = C.c_size_t()
@@ -86,9 +101,17 @@ def request_pool(n: int, seed: int, lo: int = 64, hi: int = 16384) -> list:
 def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
                 budget_bytes: int = 40 << 30, pool: int = 64, steps_lo: int = 60,
                 steps_hi: int = 600, drain_s: float = 30.0,
-                scenes_pool: Optional[list] = None) -> dict:
+                scenes_pool: Optional[list] = None,
+                max_resident_particles: int = 0) -> dict:
     """Seeded Poisson arrivals for `duration` seconds; waits up to `drain_s`
-    afterwards for outstanding requests.  Latency = submit to completion."""
+    afterwards for outstanding requests.  Latency = submit to completion.
+
+    Reported beside the latency percentiles (over completed requests): the
+    offered load (particle-substeps of every submitted request / arrival
+    window), the served throughput (particle-substeps of completed requests /
+    wall time from the first arrival to the last completion or the drain
+    limit) and their ratio; a ratio well below 1 means the arrivals exceed
+    the device's capacity and the latencies measure the backlog."""
     rng = np.random.default_rng(seed + 1)
     worlds = scenes_pool or request_pool(pool, seed)
     solvers = [w.to_solver() for w in worlds]
@@ -97,7 +120,11 @@ def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
     times = times[times < duration]
     picks = rng.integers(0, len(worlds), size=len(times))
     steps = rng.integers(steps_lo, steps_hi + 1, size=len(times))
+    units_of = np.array([int(worlds[w].n_particles) * worlds[w].sub_steps for w in picks],
+                        np.float64) * steps
     sv = Server(budget_bytes)
+    if max_resident_particles:
+        sv.set_max_resident_particles(max_resident_particles)
     sv.start()
     info = {}
     lock = threading.Lock()
@@ -110,13 +137,14 @@ def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
                 time.sleep(delay)
             rid = sv.submit(solvers[w], int(st), worlds[w].dt)
             with lock:
-                info[rid] = (k, int(worlds[w].n_particles) * worlds[w].sub_steps * int(st))
+                info[rid] = (k, float(units_of[k]))
 
     th = threading.Thread(target=submitter, daemon=True)
     th.start()
-    lat, qt, done_units = [], [], 0
+    lat, qt, done_units = [], [], 0.0
     deadline = t0 + duration + drain_s
     done = 0
+    t_last = t0
     while True:
         for rid in sv.finished():
             s, l, q = sv.take(rid)
@@ -125,25 +153,33 @@ def run_poisson(lam: float = 2000.0, duration: float = 60.0, seed: int = 0,
             with lock:
                 done_units += info[rid][1]
             done += 1
+            t_last = time.perf_counter()
             s.close()
         if not th.is_alive() and done >= len(times):
             break
         if time.perf_counter() > deadline:
+            t_last = time.perf_counter()
             break
         time.sleep(0.002)
-    wall = time.perf_counter() - t0
+    wall = t_last - t0
     stats = sv.stats()
     sv.stop()
     sv.close()
     lat_ms = np.asarray(lat) * 1e3
+    offered = float(units_of.sum()) / duration
+    served = done_units / wall if wall > 0 else 0.0
     return {
         "arrival_rate_per_s": lam, "arrival_window_s": duration, "submitted": int(len(times)),
-        "completed": done, "wall_s": wall,
+        "completed": done, "incomplete_at_drain_limit": int(len(times)) - done,
+        "drain_limit_s": drain_s, "wall_s": wall,
+        "max_resident_particles": int(max_resident_particles),
         "p50_latency_ms": float(np.percentile(lat_ms, 50)) if done else None,
         "p99_latency_ms": float(np.percentile(lat_ms, 99)) if done else None,
         "mean_queue_ms": float(np.mean(qt) * 1e3) if done else None,
-        "throughput_particle_substeps_per_s": stats["particle_substeps"] / wall,
-        "completed_particle_substeps_per_s": done_units / wall,
+        "offered_particle_substeps_per_s": offered,
+        "served_particle_substeps_per_s": served,
+        "served_over_offered": served / offered if offered > 0 else None,
+        "stepped_particle_substeps_per_s": stats["particle_substeps"] / wall if wall > 0 else 0.0,
         "ticks": stats["ticks"], "budget_bytes": budget_bytes,
         "worker_s": {"admit": stats["admit_ns"] / 1e9, "step": stats["step_ns"] / 1e9,
                      "retire": stats["retire_ns"] / 1e9},

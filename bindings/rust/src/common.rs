@@ -22,31 +22,3 @@ pub fn line_intersection(
         None
     }
 }
-
-/// Projection of `a` onto `b` (`src/common.rs:28-32`).
-#[inline]
-pub fn proj_a_on_b(a: Vector2<f32>, b: Vector2<f32>) -> Vector2<f32> {
-    a.dot(&b) / b.magnitude_squared() * b
-}
-
-/// The projection, limited to lie between zero and `b` under nalgebra's
-/// partial order of vectors (`src/common.rs:34-44`).
-#[inline]
-pub fn proj_a_on_b_clamped(a: Vector2<f32>, b: Vector2<f32>) -> Vector2<f32> {
-    let p = proj_a_on_b(a, b);
-    if p.xy() > b.xy() {
-        b
-    } else if p.xy() < Vector2::zeros() {
-        Vector2::zeros()
-    } else {
-        p
-    }
-}
-
-/// Nearest point of segment `line` to `point`, by the clamped projection
-/// (`src/common.rs:46-52`).
-#[inline]
-pub fn proj_point_on_line(point: Vector2<f32>, line: (Vector2<f32>, Vector2<f32>)) -> Vector2<f32> {
-    let (start, end) = line;
-    start + proj_a_on_b_clamped(point - start, end - start)
-}

@@ -29,6 +29,11 @@ pub const B2D_SERVE_QUEUED: c_int = 0;
 pub const B2D_SERVE_RUNNING: c_int = 1;
 pub const B2D_SERVE_DONE: c_int = 2;
 pub const B2D_SERVE_FAILED: c_int = 3;
+pub const B2D_SERVE_CANCELLED: c_int = 4;
+
+pub const B2D_FAULT_WAIT_TIMEOUT: c_int = 1;
+pub const B2D_FAULT_GRID_CAP: c_int = 2;
+pub const B2D_FAULT_ALLOC: c_int = 3;
 
 #[repr(C)]
 #[derive(Debug, Clone, Copy, Default, PartialEq)]
@@ -105,6 +110,8 @@ pub struct b2d_server_stats {
     pub admit_ns: u64,
     pub step_ns: u64,
     pub retire_ns: u64,
+    pub cancelled: u64,
+    pub resident_particles: u64,
 }
 
 /// Opaque handles.
@@ -181,6 +188,7 @@ extern "C" {
     pub fn b2d_set_tuning(s: *mut b2d_solver, key: *const c_char, value: c_double) -> c_int;
 
     pub fn b2d_update(s: *mut b2d_solver, dt: f32) -> c_int;
+    pub fn b2d_set_fault(s: *mut b2d_solver, kind: c_int, value: u64) -> c_int;
 
     pub fn b2d_get_particle_len(s: *mut b2d_solver, out: *mut usize) -> c_int;
     pub fn b2d_get_circles_len(s: *mut b2d_solver, out: *mut usize) -> c_int;
@@ -271,6 +279,9 @@ extern "C" {
     pub fn b2d_server_stop(sv: *mut b2d_server) -> c_int;
     pub fn b2d_server_submit(sv: *mut b2d_server, world: *mut b2d_solver, steps: u32, dt: f32, id: *mut u64) -> c_int;
     pub fn b2d_server_poll(sv: *mut b2d_server, id: u64, state: *mut c_int) -> c_int;
+    pub fn b2d_server_cancel(sv: *mut b2d_server, id: u64) -> c_int;
+    pub fn b2d_server_set_max_resident_particles(sv: *mut b2d_server, n: u64) -> c_int;
+    pub fn b2d_server_set_fault(sv: *mut b2d_server, kind: c_int, value: u64) -> c_int;
     pub fn b2d_server_take(
         sv: *mut b2d_server,
         id: u64,

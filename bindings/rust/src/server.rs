@@ -16,6 +16,7 @@ pub enum RequestState {
     Running,
     Done,
     Failed,
+    Cancelled,
 }
 
 /// Completion time of a taken request.
@@ -68,8 +69,21 @@ impl Server {
             ffi::B2D_SERVE_QUEUED => RequestState::Queued,
             ffi::B2D_SERVE_RUNNING => RequestState::Running,
             ffi::B2D_SERVE_DONE => RequestState::Done,
+            ffi::B2D_SERVE_CANCELLED => RequestState::Cancelled,
             _ => RequestState::Failed,
         })
+    }
+
+    /// Drops a request: a queued one at once, a running one when the tick in
+    /// flight ends.  `ffi::B2D_ERR_STATE` once it has finished.
+    pub fn cancel(&self, id: u64) -> Result<(), Error> {
+        check(unsafe { ffi::b2d_server_cancel(self.raw, id) })
+    }
+
+    /// Admission also keeps the resident solver particles at or below `n`
+    /// (0: no limit), so ticks stay short under overload.
+    pub fn set_max_resident_particles(&self, n: u64) -> Result<(), Error> {
+        check(unsafe { ffi::b2d_server_set_max_resident_particles(self.raw, n) })
     }
 
     /// Moves a finished request's world into `dst` (replacing its contents)
@@ -81,7 +95,7 @@ impl Server {
         Ok(Latency { total_s: total, queued_s: queued })
     }
 
-    /// Requests finished (done or failed) since the last call.
+    /// Requests finished (done, failed or cancelled) since the last call.
     pub fn finished(&self) -> Result<Vec<u64>, Error> {
         let mut out = Vec::new();
         let mut buf = [0u64; 256];

@@ -116,6 +116,23 @@ int b2d_set_tuning(b2d_solver* s, const char* key, double value);
 
 int b2d_update(b2d_solver* s, float dt);                    /* Solver::update, :106-116 */
 
+/* fault injection, for tests of failure detection (no counterpart in the
+ * reference, which has no failure handling): nothing here faults, traps or
+ * hangs a GPU.  B2D_FAULT_WAIT_TIMEOUT (value != 0): every executor group
+ * takes the timeout path of its first bulk-copy wait (device error word,
+ * the copy in flight still lands, the group leaves), so b2d_synchronize
+ * reports B2D_ERR_DEVICE.  B2D_FAULT_GRID_CAP (value > 0): the collision
+ * grid hands out at most `value` sorted entries per sub-step; below the
+ * particle count the scan refuses blocks instead of writing past them
+ * (B2D_ERR_DEVICE).  B2D_FAULT_ALLOC: the next `value` world-block
+ * allocations fail as if cudaMallocAsync had (B2D_ERR_CUDA).  Value 0 turns
+ * a fault off; the solver's state after a reported failure is unspecified
+ * until it is rewritten (b2d_write_state). */
+#define B2D_FAULT_WAIT_TIMEOUT 1
+#define B2D_FAULT_GRID_CAP 2
+#define B2D_FAULT_ALLOC 3
+int b2d_set_fault(b2d_solver* s, int kind, uint64_t value);
+
 int b2d_get_particle_len(b2d_solver* s, size_t* out);       /* :69-71 */
 int b2d_get_circles_len(b2d_solver* s, size_t* out);        /* :72-74 */
 int b2d_get_polygons_len(b2d_solver* s, size_t* out);       /* :75-77 */
@@ -173,11 +190,16 @@ int b2d_get_link_order(b2d_solver* s, uint64_t* order, size_t cap);
  * particles held in the caller's device arrays (pos/prev, x/y interleaved),
  * in place, on `cuda_stream` -- the same arithmetic b2d_update applies to a
  * solver holding only these particles with B2D_COLLIDE_PP.  Allocates
- * nothing: all scratch lives in one static device array of about 3.6 MB
- * (held by every GPU that loads the library until exit), so n is limited to
- * 65536 (B2D_ERR_CAPACITY beyond).  Calls share that array: calls whose GPU
- * work overlaps race.  The first call on a device resolves the array's
- * address; make it before any stream capture. */
+ * nothing: all scratch lives in one static device array of about 3.6 MB,
+ * mapped on a device when the library's kernels are first loaded there (at
+ * the latest on the first call) and held until exit, so n is limited to
+ * 65536 (B2D_ERR_CAPACITY beyond).  Calls share that array and each clears
+ * what it needs: calls whose GPU work overlaps (other streams, other
+ * threads) race.  Calls outside stream capture look the array's address up
+ * on the current device; a call under capture reuses the last one found
+ * there, so make the first call on each device before any stream capture
+ * (B2D_ERR_STATE otherwise).  Returns once the work is queued; launch
+ * failures of this call's own kernels give B2D_ERR_CUDA. */
 typedef struct {
   float gravity_x, gravity_y;
   float bounds_x, bounds_y, bounds_w, bounds_h;
@@ -219,6 +241,7 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
 #define B2D_SERVE_RUNNING 1
 #define B2D_SERVE_DONE 2
 #define B2D_SERVE_FAILED 3
+#define B2D_SERVE_CANCELLED 4
 typedef struct {
   uint64_t submitted, admitted, completed, failed, queued, active;
   uint64_t ticks, particle_substeps, resident_bytes;
@@ -226,6 +249,7 @@ typedef struct {
    * runs, + upload), stepping (launch + wait, minus that planning), retiring
    * (download + release) */
   uint64_t admit_ns, step_ns, retire_ns;
+  uint64_t cancelled, resident_particles;
 } b2d_server_stats;
 int b2d_server_create(uint64_t budget_bytes, b2d_server** out);
 int b2d_server_destroy(b2d_server* sv);
@@ -235,6 +259,18 @@ int b2d_server_stop(b2d_server* sv);
 int b2d_server_submit(b2d_server* sv, b2d_solver* world, uint32_t steps, float dt,
                       uint64_t* id);
 int b2d_server_poll(b2d_server* sv, uint64_t id, int* state);
+/* drops a request: a queued one at once, a running one when the tick in
+ * flight ends (its state becomes B2D_SERVE_CANCELLED and it is listed by
+ * b2d_server_finished); B2D_ERR_STATE once it has finished */
+int b2d_server_cancel(b2d_server* sv, uint64_t id);
+/* admission also keeps the resident solver particles at or below n, so that
+ * a tick (one update of every resident world) stays short under overload;
+ * 0 = no limit (default); one request is always admitted onto an idle device */
+int b2d_server_set_max_resident_particles(b2d_server* sv, uint64_t n);
+/* fault injection (B2D_FAULT_*, see b2d_set_fault) on the server's engine,
+ * applied before its next tick; B2D_FAULT_ALLOC fails the admission of the
+ * next `value` requests to be installed, and only those */
+int b2d_server_set_fault(b2d_server* sv, int kind, uint64_t value);
 /* moves a finished request's world into dst (replacing its contents) and
  * releases the request; latency from submit to completion, queueing time */
 int b2d_server_take(b2d_server* sv, uint64_t id, b2d_solver* dst, double* latency_s,

@@ -32,11 +32,17 @@ def kat_to_oracle(sc: dict):
         o.add_circle_link(int(a), int(b), float(r))
     for g in sc["polygons"]:
         o.add_polygon_points(np.asarray(g["points"], np.float32), g["static"])
+    for g in sc.get("polygons_full", []):  # Solver::add_polygon with given links and centre
+        o.add_polygon(np.asarray(g["pos"], np.float32), np.asarray(g["prev"], np.float32),
+                      np.asarray(g["acc"], np.float32), [tuple(l) for l in g["links"]],
+                      g["static"], tuple(g["center"]))
+    for g in sc.get("polygon_circles", []):  # Polygon::circle
+        o.add_polygon_circle(g["radius"], g["pos"][0], g["pos"][1], g["n"], g["static"])
     return o
 
 
 def kat_to_solver(sc: dict):
-    from bendy2d_gb300 import Bounds, Circle, CircleLink, Link, Particle, Solver
+    from bendy2d_gb300 import Bounds, Circle, CircleLink, Link, Particle, ParticleLink, Solver
     s = Solver()
     s.gravity = tuple(sc["gravity"])
     s.bounds = Bounds(tuple(sc["bounds"][:2]), tuple(sc["bounds"][2:]))
@@ -54,6 +60,15 @@ def kat_to_solver(sc: dict):
         s.add_circle_link(CircleLink(Link(int(a), int(b), float(r))))
     for g in sc["polygons"]:
         s.add_polygon_points([tuple(p) for p in g["points"]], g["static"])
+    from bendy2d_gb300 import Polygon
+    for g in sc.get("polygons_full", []):
+        pos, prev, acc = (np.asarray(g[k], np.float32).reshape(-1, 2) for k in ("pos", "prev", "acc"))
+        s.add_polygon(Polygon([Particle(tuple(map(float, a)), tuple(map(float, b)),
+                                        tuple(map(float, c))) for a, b, c in zip(pos, prev, acc)],
+                              [ParticleLink(Link(int(a), int(b), float(t))) for a, b, t in g["links"]],
+                              g["static"], tuple(g["center"])))
+    for g in sc.get("polygon_circles", []):
+        s.add_polygon_circle(g["radius"], tuple(g["pos"]), g["n"], g["static"])
     return s
 
 

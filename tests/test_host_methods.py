@@ -128,16 +128,11 @@ def test_link_with_bad_indices_raises(native_lib):
             ParticleLink(Link(a, b, 1.0)).solve(ps)
 
 
-def test_line_intersection_and_projections():
-    from bendy2d_gb300.api import (line_intersection, proj_a_on_b, proj_a_on_b_clamped,
-                                   proj_point_on_line)
+def test_line_intersection():
+    from bendy2d_gb300.api import line_intersection
     assert line_intersection(((0.0, 0.0), (2.0, 2.0)), ((0.0, 2.0), (2.0, 0.0))) == (1.0, 1.0)
     assert line_intersection(((0.0, 0.0), (1.0, 0.0)), ((0.0, 1.0), (1.0, 1.0))) is None  # parallel
     assert line_intersection(((0.0, 0.0), (1.0, 0.0)), ((2.0, -1.0), (2.0, 1.0))) is None
-    assert proj_a_on_b((2.0, 3.0), (4.0, 0.0)) == (2.0, 0.0)
-    assert proj_a_on_b_clamped((9.0, 9.0), (1.0, 1.0)) == (1.0, 1.0)
-    assert proj_a_on_b_clamped((-3.0, -3.0), (1.0, 1.0)) == (0.0, 0.0)
-    assert proj_point_on_line((1.0, 5.0), ((0.0, 0.0), (4.0, 0.0))) == (1.0, 0.0)
 
 
 def test_particle_forces():

@@ -142,7 +142,7 @@ def test_solver_methods_of_the_reference_are_bound():
 def test_value_type_methods_of_the_reference_are_bound():
     """The public methods of the reference's value types and its free
     functions: src/particle.rs:11-59, src/circle.rs:10-45, src/link.rs:17-48,
-    src/polygon.rs:16-229, src/common.rs:3-52."""
+    src/polygon.rs:16-229, src/common.rs:3-26."""
     expect = {
         "particle.rs": ["new", "update", "solve_bounds", "add_force", "add_force_v2",
                         "add_force_towards"],
@@ -150,8 +150,7 @@ def test_value_type_methods_of_the_reference_are_bound():
         "link.rs": ["solve"],
         "polygon.rs": ["circle", "new", "update", "solve_bounds", "solve_polygon",
                        "solve_polygon_single", "solve_links", "add_force_v2"],
-        "common.rs": ["line_intersection", "proj_a_on_b", "proj_a_on_b_clamped",
-                      "proj_point_on_line"],
+        "common.rs": ["line_intersection"],
     }
     for f, names in expect.items():
         src = (CRATE / "src" / f).read_text()

@@ -26,10 +26,10 @@ def _scene(n, box, seed):
     return pos, prev
 
 
-def _params(N, box):
+def _params(N, box, sub_steps=3, cell=1.0):
     return N.CNoAllocParams(gravity_x=0.0, gravity_y=-9.81, bounds_x=0.0, bounds_y=0.0,
-                            bounds_w=box, bounds_h=box, dt=1.0 / 60.0, sub_steps=3,
-                            particle_radius=0.5, grid_cell=1.0)
+                            bounds_w=box, bounds_h=box, dt=1.0 / 60.0, sub_steps=sub_steps,
+                            particle_radius=0.5, grid_cell=cell)
 
 
 N = None
@@ -43,8 +43,13 @@ def lib(gpu):
     return gpu
 
 
-@pytest.mark.parametrize("n,box,seed", [(5000, 60.0, 1), (40000, 100.0, 2), (65536, 180.0, 3)])
-def test_noalloc_matches_update(lib, n, box, seed):
+# odd sub-step counts end in the scratch position buffer (copied back), even
+# ones in the caller's; a cell of 1.25 takes the division path of the cell
+# coordinate, a power of two the exact reciprocal
+@pytest.mark.parametrize("n,box,seed,sub,cell", [(5000, 60.0, 1, 3, 1.0), (40000, 100.0, 2, 3, 1.0),
+                                                 (65536, 180.0, 3, 3, 1.0), (20000, 90.0, 4, 2, 1.0),
+                                                 (30000, 110.0, 5, 3, 1.25)])
+def test_noalloc_matches_update(lib, n, box, seed, sub, cell):
     import torch
     from bendy2d_gb300 import Bounds, Solver
     pos, prev = _scene(n, box, seed)
@@ -52,14 +57,14 @@ def test_noalloc_matches_update(lib, n, box, seed):
     s = Solver()
     s.gravity = (0.0, -9.81)
     s.bounds = Bounds((0.0, 0.0), (box, box))
-    s.set_sub_steps(3)
-    s.set_collision(1, 0.5, 1.0)
+    s.set_sub_steps(sub)
+    s.set_collision(1, 0.5, cell)
     s.add_particles(pos, prev)
     # no-allocation entry point on caller-owned device arrays
     d_pos = torch.from_numpy(pos.copy()).cuda()
     d_prev = torch.from_numpy(prev.copy()).cuda()
     stream = torch.cuda.current_stream()
-    prm = _params(N, box)
+    prm = _params(N, box, sub, cell)
     for call in range(2):
         s.update(1.0 / 60.0)
         code = lib.b2d_collide_substeps_noalloc(C.c_void_p(d_pos.data_ptr()),
