@@ -164,21 +164,31 @@ def run_cpu_oracle(sc, budget_s: float, max_steps: int = 1000):
     return sc.n_particles * sc.sub_steps * steps / dt, steps, dt
 
 
-def run_batched_comparison(args, torch, flush, stream):
+def run_batched_comparison(args, torch, flush, stream, world: int = 1, rank: int = 0):
     """Configuration 3: 4096 independent ring worlds (log-uniform 64..4096
     particles) stepped (a) batched: one launch sequence for all worlds, CUDA
-    graph; (b) plain: one world per launch, no graph; (c) the CPU port of the
-    reference on a sample of worlds across all host cores."""
+    graph, with the default tunables and with the ones the autotuner picks
+    on this batch; (b) plain: one world per launch, no graph; (c) the CPU
+    port of the reference on a sample of worlds across all host cores.
+    Under torchrun the worlds are sharded across ranks (sharding.shard,
+    balanced by particle-substeps, no exchange): each rank steps its shard
+    and the batched value is all worlds' particle-substeps over the slowest
+    rank's step (legs (b) and (c) run at N = 1 only)."""
     import concurrent.futures as cf
-    from bendy2d_gb300 import Batch, scenes
+    from bendy2d_gb300 import Batch, autotune, scenes
+    from bendy2d_gb300.sharding import shard, world_cost
     from oracle import load_scene
-    worlds = scenes.config3(seed=0, n_worlds=args.batched_worlds)
-    units = sum(w.n_particles * w.sub_steps for w in worlds)
+    all_worlds = scenes.config3(seed=0, n_worlds=args.batched_worlds)
+    units = sum(w.n_particles * w.sub_steps for w in all_worlds)
+    worlds = all_worlds
+    if world > 1:
+        worlds = [all_worlds[i] for i in shard([world_cost(w) for w in all_worlds], world)[rank]]
     dt = worlds[0].dt
-    out = {"workload": f"{len(worlds)} worlds of 1-8 hub-and-spoke rings, particles "
+    out = {"workload": f"{len(all_worlds)} worlds of 1-8 hub-and-spoke rings, particles "
                        "log-uniform in [64, 4096], 2 circles + floor polygon each, 8 sub-steps, "
-                       "1 link iteration (batched_i4: 4)", "worlds": len(worlds),
-           "particles": int(sum(w.n_particles for w in worlds))}
+                       "1 link iteration (batched_i4: 4)", "worlds": len(all_worlds),
+           "particles": int(sum(w.n_particles for w in all_worlds)),
+           "ranks": world, "l2": "flushed (256 MiB write) between timed steps"}
 
     def timed_steps(batch, k):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -194,17 +204,42 @@ def run_batched_comparison(args, torch, flush, stream):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in ev) / k
 
+    def slowest(ms):
+        if world == 1:
+            return ms
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
     b = Batch([w.to_solver() for w in worlds])
     b.set_stream(stream.cuda_stream)
     for _ in range(3):
         b.update(dt)
-    ms = timed_steps(b, args.batched_steps)
-    bpu = sum(step_bytes_per_unit(w) * w.n_particles for w in worlds) / \
-        max(1, sum(w.n_particles for w in worlds))
+    ms = slowest(timed_steps(b, args.batched_steps))
+    bpu = sum(step_bytes_per_unit(w) * w.n_particles for w in all_worlds) / \
+        max(1, sum(w.n_particles for w in all_worlds))
     out["batched"] = {"value": units / (ms / 1e3), "ms_per_step": ms,
                       "launches_per_step": b.launch_count(),
                       "roofline": step_roofline(units / (ms / 1e3), bpu)}
+    if world == 1 and not args.no_autotune:
+        # the autotuner re-tunes the same batch in place (every candidate is
+        # timed like the default, after a re-plan and warm-up)
+        def time_ms(r):
+            for _ in range(3):
+                r.update(dt)
+            return timed_steps(r, max(2, args.batched_steps // 2))
+        log = []
+        best = autotune.tune_runner(b, time_ms, autotune.RING_SPACE, log)
+        for _ in range(3):
+            b.update(dt)
+        ms_t = timed_steps(b, args.batched_steps)
+        out["batched_autotuned"] = {
+            "value": units / (ms_t / 1e3), "ms_per_step": ms_t,
+            "tuning": {k: v for k, v in best.items() if not k.startswith("_")},
+            "candidates_timed": len(log), "space": autotune.RING_SPACE}
     b.close()
+    if world > 1:
+        return out
     # the same worlds with 4 link iterations (batched only)
     w4 = scenes.config3(seed=0, n_worlds=args.batched_worlds, link_iters=4)
     b4 = Batch([w.to_solver() for w in w4])
@@ -522,6 +557,46 @@ def overlap_at_start(sc):
     return near_p, near_c
 
 
+def run_profile_config(args, torch) -> None:
+    """One configuration alone, for profilers: --warmup updates, then
+    --steps updates timed with CUDA events (L2 not flushed).  Launch order
+    per update is fixed, so a profiler can skip a known number of launches."""
+    from bendy2d_gb300 import Batch, MODE_FAST, scenes
+    from bendy2d_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(0)
+    k = args.profile_config
+    if k == 1:
+        sc = scenes.config1(seed=0)
+        runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
+    elif k == 2:
+        sc = build_scene(0)
+        runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
+    elif k == 3:
+        worlds = scenes.config3(seed=0, n_worlds=args.batched_worlds)
+        runner, dt = Batch([w.to_solver() for w in worlds]), worlds[0].dt
+        units = sum(w.n_particles * w.sub_steps for w in worlds)
+    else:
+        sc = scenes.config5(seed=0, mode=MODE_FAST)
+        runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
+    for _ in range(args.warmup):
+        runner.update(dt)
+    runner.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        runner.update(dt)
+    runner.synchronize()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    print(json.dumps({"profile_config": k, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": ms, "value": units / (ms / 1e3), "unit": METRIC,
+                      "launches_per_step": runner.launch_count()}))
+    runner.close()
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -541,6 +616,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuned configuration-3 batch")
     ap.add_argument("--serve-window", type=float, default=10.0,
                     help="arrival window of the stated 2,000 req/s rate (s)")
     ap.add_argument("--serve-drain", type=float, default=150.0,
@@ -555,6 +632,9 @@ def main():
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-config5", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--profile-config", type=int, choices=[1, 2, 3, 5], default=0,
+                    help="run only --warmup + --steps updates of one configuration (the "
+                         "command the ncu summaries profile) and print its step time")
     args = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -593,6 +673,9 @@ def main():
         return
 
     import torch
+    if args.profile_config:
+        run_profile_config(args, torch)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -702,6 +785,11 @@ def main():
         lv = st["levels"] / max(1, st["group_bodies"])
         chain = {"levels_per_launch": lv, "ns_per_level": dom_ms * 1e6 / lv}
 
+    # every rank steps its shard of the configuration-3 worlds
+    batched = None
+    if not args.no_batched:
+        batched = run_batched_comparison(args, torch, flush, stream, world, rank)
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -714,9 +802,6 @@ def main():
                "sample": f"{k} updates of the full workload in {el:.1f} s (C port of the "
                          "reference, single thread)"}
 
-    batched = None
-    if not args.no_batched and world == 1:
-        batched = run_batched_comparison(args, torch, flush, stream)
     config1 = None
     if not args.no_config1 and world == 1:
         config1 = run_config1_long(args, torch, stream)

@@ -12,11 +12,12 @@ updates after warm-up) and the fastest kept.  Tunables:
   stage_frac        serial bodies with chains >= this x the longest run alone,
                     links staged in shared memory
   bucket_factor     collision-grid buckets per world: pow2 >= this x particles
-Results are cached in memory by a scene signature.
+The tuning only moves work between executors and launch shapes; results are
+bit-identical whatever it picks.  Results are cached in memory by a scene
+signature.
 """
 from __future__ import annotations
 
-import time
 from typing import Callable, Optional
 
 SPACE = {
@@ -28,6 +29,24 @@ SPACE = {
     "stage_frac": [0.4, 0.67, 1.01],
     "bucket_factor": [1.0, 2.0, 4.0],
 }
+# The planner's defaults for the tunables above (PlanTuning in
+# csrc/engine.hpp); a candidate is always applied on top of these, so one
+# runner can be re-tuned in place.
+DEFAULTS = {
+    "width_per_thread": 0.5,
+    "t_max": 512,
+    "max_groups": 15,
+    "serial_width": 2.0,
+    "resident": 1,
+    "stage_frac": 0.67,
+    "bucket_factor": 2.0,
+}
+# tunables that matter for batches of chain-like worlds (rings), where the
+# serial executors carry the step
+RING_SPACE = {
+    "stage_frac": [0.4, 0.55, 0.67, 0.85, 1.01],
+    "serial_width": [1.5, 2.0, 4.0],
+}
 _CACHE: dict = {}
 
 
@@ -37,10 +56,10 @@ def signature(scenes) -> tuple:
             sc[0].sub_steps, sc[0].link_iters, sc[0].collide, sc[0].mode)
 
 
-def _time_config(make: Callable, cfg: dict, steps: int, warmup: int) -> float:
+def event_timer(runner, dt: float, steps: int, warmup: int) -> float:
+    """ms per update: `warmup` updates, then `steps` updates between CUDA
+    events on the current stream (the runner synchronises first)."""
     import torch
-    runner, dt = make()
-    runner.set_tuning(**cfg)
     for _ in range(warmup):
         runner.update(dt)
     runner.synchronize()
@@ -52,9 +71,41 @@ def _time_config(make: Callable, cfg: dict, steps: int, warmup: int) -> float:
     runner.synchronize()
     e1.record()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    runner.close()
-    return ms
+    return e0.elapsed_time(e1) / steps
+
+
+def tune_runner(runner, time_ms: Callable[[object], float], space: Optional[dict] = None,
+                log: Optional[list] = None, keep: float = 0.98) -> dict:
+    """Coordinate descent on one runner (a Solver or a Batch), re-tuned in
+    place: every candidate is the best tuning so far with one tunable
+    changed, on top of DEFAULTS.  time_ms(runner) times the current tuning
+    (warm-up included).  Returns the best tuning with its time under
+    "_ms_per_step" and leaves the runner tuned to it."""
+    space = space or SPACE
+
+    def apply(cfg: dict) -> None:
+        runner.set_tuning(**{k: cfg.get(k, DEFAULTS[k]) for k in space})
+
+    best: dict = {}
+    apply(best)
+    best_ms = time_ms(runner)
+    if log is not None:
+        log.append(({}, best_ms))
+    for name, values in space.items():
+        for v in values:
+            if v == best.get(name, DEFAULTS[name]):
+                continue
+            cfg = dict(best, **{name: v})
+            apply(cfg)
+            ms = time_ms(runner)
+            if log is not None:
+                log.append((cfg, ms))
+            if ms < best_ms * keep:
+                best, best_ms = cfg, ms
+    apply(best)
+    out = dict(best)
+    out["_ms_per_step"] = best_ms
+    return out
 
 
 def autotune(scenes, steps: int = 5, warmup: int = 3, space: Optional[dict] = None,
@@ -64,26 +115,11 @@ def autotune(scenes, steps: int = 5, warmup: int = 3, space: Optional[dict] = No
     if key in _CACHE:
         return dict(_CACHE[key])
     from .api import Batch
-
-    def make():
-        if isinstance(scenes, (list, tuple)):
-            b = Batch([s.to_solver() for s in scenes])
-            return b, scenes[0].dt
-        return scenes.to_solver(), scenes.dt
-
-    space = space or SPACE
-    best = {}
-    best_ms = _time_config(make, best, steps, warmup)
-    if log is not None:
-        log.append(({}, best_ms))
-    for name, values in space.items():
-        for v in values:
-            cfg = dict(best, **{name: v})
-            ms = _time_config(make, cfg, steps, warmup)
-            if log is not None:
-                log.append((cfg, ms))
-            if ms < best_ms * 0.98:
-                best, best_ms = cfg, ms
-    _CACHE[key] = dict(best)
-    best["_ms_per_step"] = best_ms
+    if isinstance(scenes, (list, tuple)):
+        runner, dt = Batch([s.to_solver() for s in scenes]), scenes[0].dt
+    else:
+        runner, dt = scenes.to_solver(), scenes.dt
+    best = tune_runner(runner, lambda r: event_timer(r, dt, steps, warmup), space, log)
+    runner.close()
+    _CACHE[key] = {k: v for k, v in best.items() if not k.startswith("_")}
     return best

@@ -40,6 +40,9 @@ static uint32_t pow2ceil_u(uint32_t x) {
 static int g_smem_optin = -1;
 static int g_num_sms = 0;
 static constexpr uint64_t kRigidSmemCap = 96 * 1024;
+// worlds with more pair tests than this run their circle/polygon phases in
+// 1024-thread CTAs (k_rigid<MODE, 1024>), the others in 256-thread CTAs
+static constexpr uint64_t kRigidWideTests = 4096;
 static constexpr uint32_t kSerialPackBytes = 96 * 1024;  // shared memory per small-body pack
 static constexpr uint32_t kSerialPackThreads = 64;       // bodies per serial pack
 
@@ -77,7 +80,8 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g_smem_optin = v;
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    for (auto fn : {k_rigid<0>, k_rigid<1>, k_rigid<2>, k_rigid<3>})
+    for (auto fn : {k_rigid<0, 256>, k_rigid<1, 256>, k_rigid<2, 256>, k_rigid<3, 256>,
+                    k_rigid<0, 1024>, k_rigid<1, 1024>, k_rigid<2, 1024>, k_rigid<3, 1024>})
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRigidSmemCap);
     for (auto fn : {k_exec_serial_smem<true, false>, k_exec_serial_smem<false, false>,
                     k_exec_serial_smem<true, true>, k_exec_serial_smem<false, true>})
@@ -503,6 +507,7 @@ int Engine::rebuild_lists() {
   chunks_.clear();
   rigid_full_.clear();
   rigid_ext_.clear();
+  rigid_wide_full_ = rigid_wide_ext_ = false;
   smax_ext_ = 0;
   any_pp_ = false;
   size_t np_ext = 0;
@@ -582,6 +587,12 @@ int Engine::rebuild_lists() {
         wlaunch_[si].cls.emplace_back(0u, 0u);
     }
     const bool rigid = im.params.nc > 0 || im.params.ng > 0;
+    // pair tests of the world's speculative loops: circle pairs and
+    // (edge, vertex) tests of every ordered polygon pair
+    const uint64_t rigid_tests =
+        (uint64_t)im.cpos.size() * (im.cpos.size() > 0 ? im.cpos.size() - 1 : 0) / 2 +
+        (im.stage_off.empty() ? 0 : im.stage_off.back());
+    const bool wide = rigid_tests > kRigidWideTests;
     if (rigid) {
       const uint64_t ng = im.polys.size(), nc = im.cpos.size(), nv = im.vpos.size();
       // same expression as rigid_smem_bytes() in kernels.cuh
@@ -592,10 +603,15 @@ int Engine::rebuild_lists() {
     if (full) {
       if (rigid) {
         wlaunch_[si].rigid = (int32_t)rigid_full_.size();
+        wlaunch_[si].rigid_wide = wide;
         rigid_full_.push_back(si);
+        rigid_wide_full_ |= wide;
       }
     } else {
-      if (rigid) rigid_ext_.push_back(si);
+      if (rigid) {
+        rigid_ext_.push_back(si);
+        rigid_wide_ext_ |= wide;
+      }
       smax_ext_ = std::max(smax_ext_, im.params.S);
       if (im.params.flags & COLLIDE_PP) {
         any_pp_ = true;
@@ -837,7 +853,10 @@ int Engine::launch_all(bool profiling) {
       }
       if (wl.rigid >= 0) {
         timed("plain_rigid", [&] {
-          k_rigid<0><<<1, 256, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
+          if (wl.rigid_wide)
+            k_rigid<0, 1024><<<1, 1024, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
+          else
+            k_rigid<0, 256><<<1, 256, rigid_smem_, stream_>>>(W, d_wlists_ + wl.rigid, 1, 0, rigid_smem_);
         });
       }
     }
@@ -867,7 +886,10 @@ int Engine::launch_all(bool profiling) {
   end_pass();
   if (!rigid_full_.empty()) {
     const uint32_t n = (uint32_t)rigid_full_.size();
-    timed("rigid_full", [&] { k_rigid<0><<<n, 256, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_); });
+    timed("rigid_full", [&] {
+      if (rigid_wide_full_) k_rigid<0, 1024><<<n, 1024, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_);
+      else k_rigid<0, 256><<<n, 256, rigid_smem_, ax2>>>(W, d_wlists_, n, 0, rigid_smem_);
+    });
   }
   }
   // worlds with extension collisions: per sub-step pipeline
@@ -879,8 +901,13 @@ int Engine::launch_all(bool profiling) {
     const uint32_t cur = s & 1u;
     if (nre) {  // phase B of s-1 (after collide s-1 read the circles), phase A of s
       timed("rigid_ext", [&] {
-        if (s == 0) k_rigid<1><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
-        else k_rigid<3><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        if (rigid_wide_ext_) {
+          if (s == 0) k_rigid<1, 1024><<<nre, 1024, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+          else k_rigid<3, 1024><<<nre, 1024, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        } else {
+          if (s == 0) k_rigid<1, 256><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+          else k_rigid<3, 256><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, s, rigid_smem_);
+        }
       });
     }
     begin_pass(false);
@@ -938,7 +965,10 @@ int Engine::launch_all(bool profiling) {
     if (nre) edge(stream_, ax);
   }
   if (smax_ext_ > 0) {
-    if (nre) timed("rigid_ext", [&] { k_rigid<2><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_); });
+    if (nre) timed("rigid_ext", [&] {
+      if (rigid_wide_ext_) k_rigid<2, 1024><<<nre, 1024, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_);
+      else k_rigid<2, 256><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_);
+    });
     timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
   }
   edge(ax, stream_);

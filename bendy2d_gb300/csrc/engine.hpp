@@ -205,6 +205,7 @@ class Engine {
   std::vector<LaunchClass> classes_;
   std::vector<uint2> serial_full_, serial_links_, chunks_;
   std::vector<uint32_t> rigid_full_, rigid_ext_;
+  bool rigid_wide_full_ = false, rigid_wide_ext_ = false;  // a world there has many pair tests
   uint2* d_lists_ = nullptr;
   size_t lists_cap_ = 0;
   size_t off_serial_full_ = 0, off_serial_links_ = 0, off_chunks_ = 0;
@@ -218,6 +219,7 @@ class Engine {
     uint32_t sf0 = 0, sfn = 0;                        // serial_full_
     uint32_t pk0 = 0, pkn = 0;                        // packs_full_[0].packs
     int32_t rigid = -1;                               // index into rigid_full_
+    bool rigid_wide = false;                          // 1024-thread circle/polygon CTA
   };
   // chain-like bodies packed into shared-memory CTAs (k_exec_serial_smem)
   struct SerialPacks {

@@ -688,14 +688,25 @@ __device__ __forceinline__ void calc_center(const float2* v, uint32_t n, float2&
 }
 
 // common::line_intersection, src/common.rs:3-26
+// Both parameters are quotients by the same denominator and a hit needs both
+// in [0, 1].  When a numerator's magnitude exceeds 2|den| (or it is NaN), the
+// correctly rounded quotient is at least 2 in magnitude, infinite or NaN, so
+// the test fails whatever the division returns: the divisions are skipped.
+// 2|den| is exact (or infinite on overflow, which skips nothing), so the
+// outcome is the reference's in every case.  Most pair tests of separated
+// polygons end here.
 __device__ __forceinline__ bool line_intersection(float2 p1, float2 p2, float2 p3, float2 p4,
                                                   float2& out) {
   float s1x = fsub(p2.x, p1.x), s1y = fsub(p2.y, p1.y);
   float s2x = fsub(p4.x, p3.x), s2y = fsub(p4.y, p3.y);
   float d13x = fsub(p1.x, p3.x), d13y = fsub(p1.y, p3.y);
   float den = fadd(fmul(-s2x, s1y), fmul(s1x, s2y));
-  float s = fdiv(fadd(fmul(-s1y, d13x), fmul(s1x, d13y)), den);
-  float t = fdiv(fsub(fmul(s2x, d13y), fmul(s2y, d13x)), den);
+  const float ns = fadd(fmul(-s1y, d13x), fmul(s1x, d13y));
+  const float nt = fsub(fmul(s2x, d13y), fmul(s2y, d13x));
+  const float lim = fmul(2.0f, fabsf(den));
+  if (!(fabsf(ns) <= lim && fabsf(nt) <= lim)) return false;
+  float s = fdiv(ns, den);
+  float t = fdiv(nt, den);
   if (s >= 0.0f && s <= 1.0f && t >= 0.0f && t <= 1.0f) {
     out.x = fadd(p1.x, fmul(t, s1x));
     out.y = fadd(p1.y, fmul(t, s1y));
@@ -1106,9 +1117,12 @@ __device__ __forceinline__ void rigid_phase_b(const DWorld& W, const RigidView& 
 // 2: phase B of sub-step `sub`; 3: phase B of `sub`-1, then phase A of `sub`.
 // The world's circles and polygons are staged in shared memory when they fit
 // in `smem_bytes` (serial chains then cost shared-memory latency), else the
-// phases run on global memory.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_rigid(const DWorld* __restrict__ worlds,
+// phases run on global memory.  THREADS (256 or 1024) is the window of the
+// speculative pair loops: worlds with thousands of pair tests take the wide
+// CTA (four times fewer windows and barriers, and four times the warps to
+// hide each window's latency on the one SM that runs the world).
+template <int MODE, int THREADS = 256>
+__global__ void __launch_bounds__(THREADS) k_rigid(const DWorld* __restrict__ worlds,
                                                const uint32_t* __restrict__ wlist, uint32_t n,
                                                uint32_t sub, uint32_t smem_bytes) {
   extern __shared__ __align__(16) unsigned char rsm[];

@@ -52,12 +52,13 @@ def _oracle_after(world, steps):
 
 
 def _big_world():
-    """A configuration-4-style request whose 72x72 cloth does not fit one
-    CTA's shared memory (global-memory executor), with particle collisions."""
+    """A configuration-4-style request whose 100x100 cloth (10,000 particles,
+    39,402 links) does not fit one CTA's shared memory even for the link
+    passes alone (global-memory executor), with particle collisions."""
     from bendy2d_gb300 import scenes
     from bendy2d_gb300.scenes import COLLIDE_PP
     rng = np.random.default_rng(21)
-    body = scenes.grid_body(72, 72, (300.0, 400.0), 1.0, 0.01, rng)
+    body = scenes.grid_body(100, 100, (300.0, 400.0), 1.0, 0.01, rng)
     sc = scenes._assemble("big_request", [body], bounds=(0.0, 0.0, 2000.0, 2000.0), sub_steps=8,
                           link_iters=4, collide=COLLIDE_PP)
     sc.prev = scenes._velocity_prev(sc.pos, rng, 0.5, (1.0 / 60.0) / 8.0)
