@@ -12,6 +12,8 @@ updates after warm-up) and the fastest kept.  Tunables:
   stage_frac        serial bodies with chains >= this x the longest run alone,
                     links staged in shared memory
   bucket_factor     collision-grid buckets per world: pow2 >= this x particles
+  collide_thread_min  particles in the collide pass from which it runs one
+                    thread per particle instead of three lanes each
 The tuning only moves work between executors and launch shapes; results are
 bit-identical whatever it picks.  Results are cached in memory by a scene
 signature.
@@ -28,6 +30,7 @@ SPACE = {
     "resident": [0, 1],
     "stage_frac": [0.4, 0.67, 1.01],
     "bucket_factor": [1.0, 2.0, 4.0],
+    "collide_thread_min": [0, 131072, 1 << 30],
 }
 # The planner's defaults for the tunables above (PlanTuning in
 # csrc/engine.hpp); a candidate is always applied on top of these, so one
@@ -40,6 +43,7 @@ DEFAULTS = {
     "resident": 1,
     "stage_frac": 0.67,
     "bucket_factor": 2.0,
+    "collide_thread_min": 131072,
 }
 # tunables that matter for batches of chain-like worlds (rings), where the
 # serial executors carry the step

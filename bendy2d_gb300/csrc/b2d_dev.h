@@ -19,6 +19,11 @@ namespace b2d {
 
 // Collision extension flags (not in the reference; see solve_dynamic_collisions).
 enum : uint32_t { COLLIDE_PP = 1u, COLLIDE_PC = 2u, COLLIDE_PPOLY = 4u };
+// World flag set by the planner: every solver particle of this world belongs
+// to a body that the shared-memory link executor runs, so that executor
+// enters each particle into the collision grid's counting pass as it stores
+// the body back (no separate count kernel for this world).
+constexpr uint32_t GRID_IN_LINKS = 8u;
 
 // Schedule op encoding: link ops carry the body-local link index; bounds +
 // integrate ops carry the body-local particle index with this bit set.

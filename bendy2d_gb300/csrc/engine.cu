@@ -510,6 +510,7 @@ int Engine::rebuild_lists() {
   rigid_wide_full_ = rigid_wide_ext_ = false;
   smax_ext_ = 0;
   any_pp_ = false;
+  any_count_ = false;
   size_t np_ext = 0;
   size_t nbuckets = 0, np_pp = 0;
   uint64_t rigid_smem = 0;
@@ -618,6 +619,7 @@ int Engine::rebuild_lists() {
         // this world's bucket range: a power of two >= 2 x its particles
         const uint32_t nbw = pow2ceil_u(std::max<uint32_t>(
             (uint32_t)(tune_.bucket_factor * (float)im.params.np), 64u));
+        if (!(im.params.flags & GRID_IN_LINKS)) any_count_ = true;
         if (h_worlds_[si].gb0 != (uint32_t)nbuckets || h_worlds_[si].gmask != nbw - 1 ||
             h_worlds_[si].gp0 != (uint32_t)np_pp) {
           h_worlds_[si].gb0 = (uint32_t)nbuckets;
@@ -704,7 +706,7 @@ int Engine::rebuild_lists() {
   if (!wl.empty())
     B2D_CUDA(cudaMemcpyAsync(d_wlists_, wl.data(), wl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
   B2D_CUDA(cudaStreamSynchronize(stream_));
-  (void)np_ext;
+  collide_per_particle_ = np_ext >= tune_.collide_thread_min;
   if (nbuckets > 0) {
     int st = ensure_grid(nbuckets, np_pp);
     if (st != OK) return st;
@@ -808,11 +810,12 @@ int Engine::launch_all(bool profiling) {
     // filled every SM and delayed that branch: 18 % slower on 1,024 bodies.)
     const bool pdl = !profiling && !c.full && c.res && st == stream_;
     void (*k)(const DWorld*, DScheds, const uint2*, uint32_t, uint32_t, uint32_t, uint32_t,
-              uint32_t, uint32_t, uint32_t) =
+              uint32_t, uint32_t, uint32_t, uint32_t*, uint2*) =
         c.res ? (c.full ? k_exec_groups<true, true, true> : k_exec_groups<false, true, true>)
         : c.full ? (c.smem ? k_exec_groups<true, true, false> : k_exec_groups<true, false, false>)
                  : (c.smem ? k_exec_groups<false, true, false> : k_exec_groups<false, false, false>);
-    lk(launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub));
+    lk(launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub, GR.count,
+                GR.pbr));
   };
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
@@ -939,10 +942,12 @@ int Engine::launch_all(bool profiling) {
       const bool small = grid_used_ <= SCAN_SMALL_MAX;
       const uint32_t tile = small ? SCAN_SMALL_TILE : SCAN_LARGE_TILE;
       const uint32_t nt = (grid_used_ + tile - 1) / tile;
-      timed("grid_count", [&] {
-        lk(launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GR, CH,
-                    nch, cur, s));
-      });
+      // worlds whose link executor counted their particles skip this pass
+      if (any_count_)
+        timed("grid_count", [&] {
+          lk(launch_k(k_grid_count, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GR, CH,
+                      nch, cur, s));
+        });
       const uint32_t ncta = small ? nt : std::min<uint32_t>(nt, (uint32_t)std::max(g_num_sms, 1));
       timed("grid_scan", [&] {
         if (small)
@@ -959,8 +964,12 @@ int Engine::launch_all(bool profiling) {
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      lk(launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0,
-                  stream_, !profiling, W, GR, CH, nch, cur, s));
+      if (collide_per_particle_)
+        lk(launch_k(k_collide_particle, dim3(nch), dim3(COLLIDE_P_THREADS), 0, stream_,
+                    !profiling, W, GR, CH, nch, cur, s));
+      else
+        lk(launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0,
+                    stream_, !profiling, W, GR, CH, nch, cur, s));
     });
     if (nre) edge(stream_, ax);
   }

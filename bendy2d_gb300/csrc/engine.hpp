@@ -42,6 +42,8 @@ struct PlanTuning {
   uint32_t res_max = 227 * 1024;    // shared bytes per group for body + resident schedule
   float stage_frac = 0.67f;         // serial bodies with chains >= this x the longest: solo packs
   float bucket_factor = 2.0f;       // collision-grid buckets per world: pow2 >= this x particles
+  uint32_t collide_thread_min = 131072;  // particles in the collide pass from which it runs
+                                         // one thread per particle (else three lanes each)
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };
@@ -235,6 +237,8 @@ class Engine {
                    bool allow_large);
   std::vector<WorldLaunch> wlaunch_;
   bool any_pp_ = false;
+  bool any_count_ = false;  // a world with particle collisions needs the count kernel
+  bool collide_per_particle_ = false;  // k_collide_particle instead of k_collide_integrate
   uint32_t rigid_smem_ = 0;
   uint32_t grid_used_ = 0;
   size_t grid_bytes_ = 0;

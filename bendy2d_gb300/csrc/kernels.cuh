@@ -104,6 +104,36 @@ __device__ __forceinline__ void integrate(float2& p, float2& q, float ax, float 
   p.y = fadd(fadd(p.y, vy), fmul(fmul(ay, h), h));
 }
 
+// ----------------------------------------------------------------------------
+// Extension collision grid: cells and buckets (used by the grid kernels below
+// and by the link executor's counting store-back).
+// ----------------------------------------------------------------------------
+// Cell index along one axis: floor((p - origin) / cell), clamped.  For a
+// power-of-two cell the division is the multiplication by icell (exact, the
+// same bits); otherwise icell is 0 and the IEEE division runs.
+__device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell, float icell) {
+  const float t = fsub(p, origin);
+  float v = floorf(icell != 0.0f ? fmul(t, icell) : fdiv(t, cell));
+  if (!(v > -1.0e9f)) v = -1.0e9f;
+  if (v > 1.0e9f) v = 1.0e9f;
+  return (int32_t)v;
+}
+__device__ __forceinline__ uint32_t cell_hash(int32_t cx, int32_t cy) {
+  uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u);
+  h ^= h >> 15;
+  h *= 0x2c1b3c6du;
+  h ^= h >> 12;
+  return h;
+}
+// Bucket of cell (cx, cy) in world W: four horizontally adjacent cells (a
+// strip, cx >> 2) hash together and take four consecutive buckets, so a row
+// of neighbour cells lands in one or two runs of `sorted` and its range and
+// entry loads mostly share cache lines.  (The world's bucket count is a
+// power of two >= 64, so the mask keeps the low two bits.)
+__device__ __forceinline__ uint32_t bucket_of(const DWorld& W, int32_t cx, int32_t cy) {
+  return W.gb0 + (((cell_hash(cx >> 2, cy) << 2) | ((uint32_t)cx & 3u)) & W.gmask);
+}
+
 // Group barrier: a group is one warp (syncwarp) or a named barrier over T
 // threads.  Both order shared and global memory among the group's threads.
 __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
@@ -229,7 +259,8 @@ template <bool FULL, bool SMEM, bool RES>
 __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
                               uint32_t G, uint32_t region_bytes, uint32_t sched_bytes,
-                              uint32_t cur, uint32_t sub) {
+                              uint32_t cur, uint32_t sub, uint32_t* __restrict__ gcount,
+                              uint2* __restrict__ gpbr) {
   extern __shared__ __align__(128) unsigned char smem[];
   pdl_trigger();
   const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
@@ -474,6 +505,20 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   if (SMEM) {
     const float2* sp = reinterpret_cast<const float2*>(base);
     const float2* sq = sp + B.np;
+    if (!FULL && (W.flags & GRID_IN_LINKS)) {
+      // store back and enter each particle into the grid's counting pass
+      // (what k_grid_count does for other worlds): its bucket, and its rank
+      // in the bucket from the counter
+      for (uint32_t i = t; i < B.np; i += T) {
+        const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
+        const float2 p = sp[i];
+        gp[k] = p;
+        const uint32_t b = bucket_of(W, cell_coord(p.x, W.bx, W.cell, W.icell),
+                                     cell_coord(p.y, W.by, W.cell, W.icell));
+        gpbr[W.gp0 + k] = make_uint2(b, atomicAdd(&gcount[b], 1u));
+      }
+      return;
+    }
 #pragma unroll 4
     for (uint32_t i = t; i < B.np; i += T) {
       const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
@@ -1166,32 +1211,6 @@ __global__ void __launch_bounds__(THREADS) k_rigid(const DWorld* __restrict__ wo
 // particle of the 9 surrounding cells, summed in fixed point so that the
 // result does not depend on the visiting order.
 // ----------------------------------------------------------------------------
-// Cell index along one axis: floor((p - origin) / cell), clamped.  For a
-// power-of-two cell the division is the multiplication by icell (exact, the
-// same bits); otherwise icell is 0 and the IEEE division runs.
-__device__ __forceinline__ int32_t cell_coord(float p, float origin, float cell, float icell) {
-  const float t = fsub(p, origin);
-  float v = floorf(icell != 0.0f ? fmul(t, icell) : fdiv(t, cell));
-  if (!(v > -1.0e9f)) v = -1.0e9f;
-  if (v > 1.0e9f) v = 1.0e9f;
-  return (int32_t)v;
-}
-__device__ __forceinline__ uint32_t cell_hash(int32_t cx, int32_t cy) {
-  uint32_t h = ((uint32_t)cx * 73856093u) ^ ((uint32_t)cy * 19349663u);
-  h ^= h >> 15;
-  h *= 0x2c1b3c6du;
-  h ^= h >> 12;
-  return h;
-}
-// Bucket of cell (cx, cy) in world W: four horizontally adjacent cells (a
-// strip, cx >> 2) hash together and take four consecutive buckets, so a row
-// of neighbour cells lands in one or two runs of `sorted` and its range and
-// entry loads mostly share cache lines.  (The world's bucket count is a
-// power of two >= 64, so the mask keeps the low two bits.)
-__device__ __forceinline__ uint32_t bucket_of(const DWorld& W, int32_t cx, int32_t cy) {
-  return W.gb0 + (((cell_hash(cx >> 2, cy) << 2) | ((uint32_t)cx & 3u)) & W.gmask);
-}
-
 // particles per work chunk: one CTA of the count / scatter / copy-back
 // kernels, four collide CTAs of 8 warps x 10 particles
 constexpr uint32_t CHUNK = 320;
@@ -1207,11 +1226,10 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   const uint2 ch = chunks[blockIdx.x < nchunks ? blockIdx.x : 0u];
   const DWorld& W = worlds[ch.x];
   const uint32_t j = ch.y + threadIdx.x;
-  const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S && (W.flags & COLLIDE_PP);
+  const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S &&
+                   (W.flags & (COLLIDE_PP | GRID_IN_LINKS)) == COLLIDE_PP;
   const float2* P = W.pos[cur];
   pdl_wait();  // positions from the link phase
-  // the previous sub-step's scatter and collide are done with the cursor
-  if (blockIdx.x == 0 && threadIdx.x == 0) *G.cursor = 0u;
   if (!act) return;
   const float2 p = P[j];
   const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
@@ -1265,9 +1283,9 @@ __device__ __forceinline__ uint4 block_exclusive_scan4(uint4 v, uint4* total) {
 // collide pass's loads together), but the tiles land in `sorted` in the order
 // their atomics ran.  Nothing reads that order: the contact sums are exact
 // integer sums, so the order of a bucket's entries does not matter either
-// (it already follows the count pass's atomics).  The count pass reset the
-// cursor; a block that would end past `cap` (a cursor left over from a failed
-// launch) is not handed out: its buckets get empty ranges and
+// (it already follows the count pass's atomics).  The previous sub-step's
+// collide kernel reset the cursor; a block that would end past `cap` (a
+// cursor left over from a failed launch) is not handed out: its buckets get empty ranges and
 // ERR_BIT_GRID_OVERFLOW is set.  The scan also zeroes the counts it read,
 // leaving them ready for the next sub-step's count pass.  Within a tile,
 // thread t holds buckets 4t .. 4t+3 of each sub-tile, so every load and
@@ -1277,7 +1295,7 @@ __global__ void __launch_bounds__(THREADS) k_grid_scan(DGrid G, uint32_t nbucket
   constexpr uint32_t SUB = 4u * THREADS;
   __shared__ uint32_t s_base, s_ok;
   pdl_trigger();
-  pdl_wait();  // counts and the cursor reset from the count pass
+  pdl_wait();  // counts from the count pass or the link executor
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     // bucket ranges are whole multiples of 64, so each group of four counts
     // is either all inside or all outside
@@ -1535,6 +1553,10 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate
   const uint2 ch = chunks[cidx < nchunks ? cidx : 0u];
   const DWorld& W = worlds[ch.x];
   pdl_wait();  // sorted entries from the scatter (and everything before it)
+  // this sub-step's scan is done with the cursor: clear it for the next one
+  // (whose scan runs after this kernel completes).  Engines without particle
+  // collisions have no grid (null cursor) but still run this kernel.
+  if (blockIdx.x == 0 && threadIdx.x == 0 && G.cursor != nullptr) *G.cursor = 0u;
   if (cidx >= nchunks || sub >= W.S) return;  // uniform over the CTA
   const uint32_t wl = threadIdx.x & 31u, grp = wl / 3u, row = wl - 3u * grp;
   const uint32_t i = ch.y + (blockIdx.x % COLLIDE_CTAS) * (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP) +
@@ -1596,6 +1618,104 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate
         const float R = W.radius + W.crad[k];
         near |= !(separated(c.x - R, c.x + R, box.x, box.z) ||
                   separated(c.y - R, c.y + R, box.y, box.w));
+      }
+    }
+    if (flags & COLLIDE_PPOLY) {
+      for (uint32_t k = wl; k < W.ng; k += 32u) {
+        const float4 bb = W.paabb[k];
+        const float r = W.radius;
+        near |= !(separated(bb.x - r, bb.z + r, box.x, box.z) ||
+                  separated(bb.y - r, bb.w + r, box.y, box.w));
+      }
+    }
+    if (__any_sync(0xFFFFFFFFu, near) && own) {
+      if (flags & COLLIDE_PC) p = particle_circles(W, p);
+      if (flags & COLLIDE_PPOLY) {
+        for (uint32_t k = 0; k < W.ng; ++k) p = particle_polygon(W, k, p);
+      }
+    }
+  }
+  if (!own) return;
+  solve_bounds(p, q, W);
+  integrate(p, q, W.gx, W.gy, W.h);
+  W.pos[cur ^ 1u][i] = p;
+  W.prev[i] = q;
+}
+
+// The same sub-step with one thread per particle, which walks all nine
+// neighbour cells itself (the nine bucket ranges loaded first, together):
+// about half the instructions per particle of the three-lane form, for
+// launches with many waves of particles, where the collide pass is bound by
+// instruction issue (configuration 5: 2.68 -> 1.98 ms per update); with few
+// waves the three-lane form's shorter chains win (configuration 2: 0.17
+// against 0.24 ms).  Same contacts and the same fixed-point sums, so the
+// same bits.  One CTA per work chunk.
+constexpr uint32_t COLLIDE_P_THREADS = CHUNK;
+static __global__ void __launch_bounds__(COLLIDE_P_THREADS, 3) k_collide_particle(
+    const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
+    uint32_t nchunks, uint32_t cur, uint32_t sub) {
+  pdl_trigger();
+  // chunk and world records are fixed during a step: read before the wait
+  const uint32_t cidx = blockIdx.x;
+  const uint2 ch = chunks[cidx < nchunks ? cidx : 0u];
+  const DWorld& W = worlds[ch.x];
+  pdl_wait();  // sorted entries from the scatter (and everything before it)
+  // as in k_collide_integrate: the scan is done with the cursor
+  if (blockIdx.x == 0 && threadIdx.x == 0 && G.cursor != nullptr) *G.cursor = 0u;
+  if (cidx >= nchunks || sub >= W.S) return;  // uniform over the CTA
+  const uint32_t wl = threadIdx.x & 31u;
+  const uint32_t i = ch.y + threadIdx.x;
+  const bool own = i < W.np;
+  const float2* P = W.pos[cur];
+  float2 p = own ? P[i] : make_float2(0.f, 0.f);
+  float2 q = own ? W.prev[i] : make_float2(0.f, 0.f);  // issued early, used last
+  if (W.flags & COLLIDE_PP) {  // uniform over the CTA
+    Contacts c;
+    c.n = 0;
+    c.sx = 0;
+    c.sy = 0;
+    c.hit = false;
+    if (own) {
+      const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell);
+      const int32_t cy0 = cell_coord(p.y, W.by, W.cell, W.icell);
+      const float D = fadd(W.radius, W.radius);
+      const float D2 = fmul(D, D);
+      // buckets of cells cx - 1 .. cx + 1 in each row, as k_collide_integrate
+      const int32_t st = cx >> 2;
+      const uint32_t k = (uint32_t)cx & 3u;
+      uint2 r[9];
+#pragma unroll
+      for (int row = 0; row < 3; ++row) {
+        const int32_t cy = cy0 + row - 1;
+        const uint32_t hm = (cell_hash(st, cy) << 2) & W.gmask;
+        const uint32_t ho = (cell_hash(k == 0u ? st - 1 : st + 1, cy) << 2) & W.gmask;
+        r[3 * row] = G.range[W.gb0 + (k == 0u ? (ho | 3u) : (hm | (k - 1u)))];
+        r[3 * row + 1] = G.range[W.gb0 + (hm | k)];
+        r[3 * row + 2] = G.range[W.gb0 + (k == 3u ? ho : (hm | (k + 1u)))];
+      }
+#pragma unroll
+      for (int row = 0; row < 3; ++row)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          visit_cell(G, p, cx + j - 1, cy0 + row - 1, r[3 * row + j].x, r[3 * row + j].y, D, D2,
+                     c);
+      contacts_finish(D, c);
+      if (c.hit) {
+        p.x = fadd(p.x, unfix32(c.sx));
+        p.y = fadd(p.y, unfix32(c.sy));
+      }
+    }
+  }
+  const uint32_t flags = W.flags;
+  if (flags & (COLLIDE_PC | COLLIDE_PPOLY)) {  // per-warp filter, as k_collide_integrate
+    const float4 box = warp_box(own, p);
+    bool near = false;
+    if (flags & COLLIDE_PC) {
+      for (uint32_t k = wl; k < W.nc; k += 32u) {
+        const float2 cc = W.cpos[k];
+        const float R = W.radius + W.crad[k];
+        near |= !(separated(cc.x - R, cc.x + R, box.x, box.z) ||
+                  separated(cc.y - R, cc.y + R, box.y, box.w));
       }
     }
     if (flags & COLLIDE_PPOLY) {

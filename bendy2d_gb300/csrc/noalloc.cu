@@ -14,8 +14,9 @@
 // until the process exits.  Every call shares it and it keeps the previous
 // call's contents, so each call clears what must start at zero; calls whose
 // GPU work overlaps (different streams, or host threads racing) corrupt each
-// other.  The scan's cursor lives there too (the count pass resets it every
-// sub-step); a range past the scratch entries would be refused and recorded
+// other.  The scan's cursor lives there too (cleared at the start of every
+// call and by each sub-step's collide kernel); a range past the scratch
+// entries would be refused and recorded
 // as ERR_BIT_GRID_OVERFLOW in a scratch word (O_ERR) that a debugger can
 // read, since this asynchronous call returns before the GPU work runs.
 //
@@ -180,6 +181,8 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
   // covers a call that stopped part-way)
   if ((e = cudaMemsetAsync(G.count, 0, (size_t)nb * 4, st)) != cudaSuccess)
     return bad(e, "clearing the bucket counts");
+  if ((e = cudaMemsetAsync(G.cursor, 0, 4, st)) != cudaSuccess)
+    return bad(e, "clearing the scan cursor");
   for (uint32_t s = 0; s < w.S; ++s) {
     const uint32_t cur = s & 1u;
     if ((e = launch(k_grid_count, nch, CHUNK, st, (const DWorld*)dW, G, (const uint2*)chunks, nch,

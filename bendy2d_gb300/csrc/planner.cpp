@@ -42,6 +42,7 @@ bool PlanTuning::set(const std::string& k, double v) {
   else if (k == "res_max") res_max = (uint32_t)v;
   else if (k == "stage_frac") stage_frac = (float)v;
   else if (k == "bucket_factor") bucket_factor = (float)v;
+  else if (k == "collide_thread_min") collide_thread_min = (uint32_t)v;
   else return false;
   return true;
 }
@@ -438,6 +439,13 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
   }
   P.nb = (uint32_t)im.bodies.size();
   im.stats.bodies = P.nb;
+  // particle collisions with every particle in a shared-memory group body:
+  // the link executor counts them into the grid (GRID_IN_LINKS)
+  if ((P.flags & COLLIDE_PP) && free_parts.empty() && im.serials.empty() && np > 0) {
+    bool all_smem = true;
+    for (const GroupBody& gb : im.groups) all_smem = all_smem && gb.smem;
+    if (all_smem) P.flags |= GRID_IN_LINKS;
+  }
 
   // circles (src/circle.rs:4-8) and circle links
   for (const Circle& c : w.circles) {

@@ -109,7 +109,8 @@ int b2d_set_collision(b2d_solver* s, uint32_t flags, float particle_radius, floa
 int b2d_set_circle_static(b2d_solver* s, size_t index, int is_static);
 /* executor tunables (the autotuner sets these): serial_width, t_min, t_max,
  * pack_np, pack_nl, free_chunk, smem_max, warp_groups, max_groups,
- * width_per_thread, resident, res_max, stage_frac, bucket_factor; they move
+ * width_per_thread, resident, res_max, stage_frac, bucket_factor,
+ * collide_thread_min; they move
  * work between executors and never change results; take effect at the next
  * update; B2D_ERR_ARG for an unknown key */
 int b2d_set_tuning(b2d_solver* s, const char* key, double value);

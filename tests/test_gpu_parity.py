@@ -101,6 +101,24 @@ def test_collision_flag_combinations(gpu, collide):
     check(sc, 6, f"collide={collide}")
 
 
+@pytest.mark.parametrize("collide", [1, 3, 7])
+def test_per_particle_collide_matches_oracle(gpu, collide):
+    """The collide pass with one thread per particle (taken by large
+    launches; forced here with collide_thread_min = 0) against the oracle,
+    with particle-particle contacts alone and with circles and polygons."""
+    from bendy2d_gb300 import scenes
+    sc = scenes.config2(seed=20 + collide, n_bodies=5, box=100.0, n_circles=5, n_polys=3,
+                        collide=collide)
+    s = sc.to_solver()
+    s.set_tuning(collide_thread_min=0)
+    from oracle import load_scene
+    o = load_scene(sc)
+    for _ in range(6):
+        s.update(sc.dt)
+        assert o.update(sc.dt) == 0
+    assert_same_state(solver_state(s), oracle_state(o), f"per-particle collide, collide={collide}")
+
+
 def test_fast_mode_matches_oracle_in_colour_order(gpu):
     from bendy2d_gb300 import MODE_FAST, scenes
     sc = scenes.config1(seed=3)
@@ -389,7 +407,7 @@ def test_config5_full_size_isolated_bodies_match_oracle(gpu):
     {"t_max": 64}, {"t_min": 256, "t_max": 256}, {"width_per_thread": 2.0},
     {"resident": 0}, {"serial_width": 1000.0}, {"serial_width": 0.0},
     {"max_groups": 1, "warp_groups": 1}, {"stage_frac": 0.0}, {"stage_frac": 2.0},
-    {"smem_max": 16384},
+    {"smem_max": 16384}, {"collide_thread_min": 0},
 ])
 def test_tunables_never_change_results(gpu, tuning):
     """Executor tunables move work between executors, group sizes, launch
