@@ -61,7 +61,7 @@ class CPlanStats(C.Structure):
     _fields_ = [("bodies", C.c_uint32), ("group_bodies", C.c_uint32),
                 ("serial_bodies", C.c_uint32), ("global_bodies", C.c_uint32),
                 ("levels", C.c_uint64), ("ops", C.c_uint64), ("colours", C.c_uint32),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("large_bodies", C.c_uint32)]
 
 
 _P = C.c_void_p

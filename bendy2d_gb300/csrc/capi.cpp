@@ -624,6 +624,7 @@ int b2d_get_plan_stats(b2d_solver* s, b2d_plan_stats* out) {
   out->levels = im->stats.levels;
   out->ops = im->stats.ops;
   out->colours = im->stats.colours;
+  out->large_bodies = im->stats.large_bodies;
   return OK;
 }
 int b2d_get_link_order(b2d_solver* s, uint64_t* order, size_t cap) {

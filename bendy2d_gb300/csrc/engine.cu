@@ -86,6 +86,11 @@ Engine::Engine(cudaStream_t stream) : stream_(stream) {
     for (auto fn : {k_exec_serial_smem<true, false>, k_exec_serial_smem<false, false>,
                     k_exec_serial_smem<true, true>, k_exec_serial_smem<false, true>})
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    for (auto fn : {k_exec_large<true, true>, k_exec_large<false, true>,
+                    k_exec_large<true, false>, k_exec_large<false, false>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    for (auto fn : {k_exec_large<true, true>, k_exec_large<false, true>})
+      cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     for (auto fn : {k_exec_groups<true, true, false>, k_exec_groups<false, true, false>,
                     k_exec_groups<true, false, false>, k_exec_groups<false, false, false>,
                     k_exec_groups<true, true, true>, k_exec_groups<false, true, true>})
@@ -548,7 +553,9 @@ int Engine::rebuild_lists() {
       const bool use_res =
           gb.res && res_count[std::make_tuple(gb.T, full, log2c(gb.region + gb.res))] <=
                         (size_t)std::max(g_num_sms, 1);
-      const uint32_t bin = gb.smem ? log2c(gb.region + (use_res ? gb.res : 0u)) : 0u;
+      // large-body classes are keyed by their cluster layout instead of a bin
+      const uint32_t bin = gb.large_c ? (0x10000u | (gb.large_c << 8) | gb.log2per)
+                           : gb.smem ? log2c(gb.region + (use_res ? gb.res : 0u)) : 0u;
       auto key = std::make_tuple(gb.T, gb.smem, full, use_res, bin);
       auto it = cls.find(key);
       if (it == cls.end()) {
@@ -561,6 +568,8 @@ int Engine::rebuild_lists() {
         c.fill = 0;
         c.words = 0;
         c.G = 1;
+        c.large_c = gb.large_c;
+        c.log2per = gb.log2per;
         it = cls.emplace(key, classes_.size()).first;
         classes_.push_back(std::move(c));
       }
@@ -638,6 +647,7 @@ int Engine::rebuild_lists() {
   // size each class to its largest member; a resident class whose largest
   // body and largest schedule do not fit together streams instead
   for (LaunchClass& c : classes_) {
+    if (c.large_c) continue;  // one body per cluster, shared memory set by its layout
     if (c.res && (size_t)c.region + c.res + GROUP_TAIL_BYTES > (size_t)g_smem_optin) c.res = 0;
     // streamed: one 16 KB chunk per fill, or for launches with no more bodies
     // than SMs (latency-bound) the largest fills that fit beside the body,
@@ -799,6 +809,26 @@ int Engine::launch_all(bool profiling) {
   // one launch of a group class over n work items starting at L
   auto launch_class = [&](const LaunchClass& c, const uint2* L, uint32_t n, uint32_t cur,
                           uint32_t sub, cudaStream_t st) {
+    if (c.large_c) {  // large-body executor: one cluster of large_c CTAs per body
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(n * c.large_c);
+      cfg.blockDim = dim3(c.T);
+      cfg.dynamicSmemBytes = (size_t)(c.full ? 16u : 8u) << c.log2per;
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c.large_c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = c.large_c > 1 ? 1u : 0u;
+      void (*kl)(const DWorld*, DScheds, const uint2*, uint32_t, uint32_t, uint32_t, uint32_t,
+                 uint32_t) =
+          c.full ? (c.large_c > 1 ? k_exec_large<true, true> : k_exec_large<true, false>)
+                 : (c.large_c > 1 ? k_exec_large<false, true> : k_exec_large<false, false>);
+      lk(cudaLaunchKernelEx(&cfg, kl, W, SC, L, n, c.large_c, c.log2per, cur, sub));
+      return;
+    }
     const dim3 grid((n + c.G - 1) / c.G), block(c.T * c.G);
     const uint32_t sb = c.res ? c.res : 2 * c.fill;
     const size_t sm = (size_t)c.G * (c.region + sb + GROUP_TAIL_BYTES);
@@ -820,8 +850,9 @@ int Engine::launch_all(bool profiling) {
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
       if (c.full != full || c.items.empty()) continue;
-      const char* name = full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
-                              : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
+      const char* name = c.large_c ? (full ? "exec_large_full" : "exec_large_links")
+                         : full ? (c.smem ? "exec_groups_full_smem" : "exec_groups_full_global")
+                                : (c.smem ? "exec_groups_links_smem" : "exec_groups_links_global");
       const cudaStream_t st = branch();
       timed(name, [&] { launch_class(c, d_lists_ + c.dev_off, (uint32_t)c.items.size(), cur, sub, st); });
     }

@@ -44,6 +44,8 @@ struct PlanTuning {
   float bucket_factor = 2.0f;       // collision-grid buckets per world: pow2 >= this x particles
   uint32_t collide_thread_min = 131072;  // particles in the collide pass from which it runs
                                          // one thread per particle (else three lanes each)
+  uint32_t large_max = 8;           // largest cluster of the large-body executor (0: bodies
+                                    // over one CTA's shared memory run from global memory)
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };
@@ -63,11 +65,14 @@ struct GroupBody {
   uint32_t region;  // shared bytes for this body (0 when run from global memory)
   uint32_t res;     // bytes of its schedule when held whole in shared memory, else 0
   bool smem;
+  uint32_t large_c = 0;  // large-body executor: CTAs in the body's cluster (0: not used)
+  uint32_t log2per = 0;  // large-body executor: log2 of the particles per CTA
 };
 
 
 struct PlanStats {
   uint32_t bodies = 0, group_bodies = 0, serial_bodies = 0, global_bodies = 0;
+  uint32_t large_bodies = 0;  // group bodies run by the large-body executor
   uint64_t levels = 0, ops = 0;  // summed over group bodies
   uint32_t colours = 0;
 };
@@ -117,6 +122,7 @@ struct LaunchClass {
   uint32_t fill;   // streamed: bytes per fill buffer (two per group)
   uint32_t words;  // largest member schedule, in words
   bool smem, full;
+  uint32_t large_c = 0, log2per = 0;  // large-body executor class (large_c CTAs per body)
   std::vector<uint2> items;
   size_t dev_off = 0;  // offset (in uint2) into the device list buffer
 };

@@ -529,6 +529,139 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 }
 
 // ----------------------------------------------------------------------------
+// Large-body executor: bodies whose state, link parameters and schedule do
+// not fit one CTA's shared memory together, which the group executor would
+// run from global memory (measured 2.4-4x slower per level than with the
+// body in shared memory).  Here the body's positions (and previous
+// positions, whole-step form) stay in shared memory, split over the C CTAs
+// of a thread-block cluster (C = 1 when they fit one CTA): particle j lives
+// in CTA j >> log2per at slot j & (per - 1), and every thread of the cluster
+// reaches it through distributed shared memory (mapa + ld/st
+// .shared::cluster).  Link parameters and the level schedule are read from
+// global memory through the caches (they are never written during a step).
+// A segment's ops go to the cluster's C*T threads in turn, and a cluster
+// barrier (release / acquire) follows every segment, so each level sees
+// the stores of the one before.  Nothing waits but those barriers, which
+// every thread of the cluster reaches through the same sequence of
+// segments (the schedule does not depend on the data), so no wait can hang.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// all threads of the cluster (the non-.aligned form: threads need not be
+// converged when they arrive)
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+// the address of the same shared-memory offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t dsmem_addr(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float2 ldc_f32x2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void stc_f32x2(uint32_t a, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+
+template <bool FULL, bool CLUSTER>
+__global__ void __launch_bounds__(1024) k_exec_large(const DWorld* __restrict__ worlds, DScheds SC,
+                                                     const uint2* __restrict__ list, uint32_t nlist,
+                                                     uint32_t C, uint32_t log2per, uint32_t cur,
+                                                     uint32_t sub) {
+  extern __shared__ __align__(16) unsigned char lsm[];
+  // with cluster dimensions (C, 1, 1) the C consecutive CTAs of an item form
+  // its cluster; every early return below is uniform over the cluster
+  const uint32_t item = blockIdx.x / C;
+  if (item >= nlist) return;
+  const uint32_t rank = CLUSTER ? cluster_rank() : 0u;
+  const uint2 wi = list[item];
+  const DWorld& W = worlds[wi.x];
+  if (!FULL && sub >= W.S) return;  // world already finished its sub-steps
+  const DBody B = W.bodies[wi.y];
+  const DSched S = SC.scheds[B.sched];
+  const uint32_t* bidx = W.bidx + B.i0;
+  float2* gp = W.pos[cur];
+  float2* gq = W.prev;
+  const uint2* gab = W.lab + B.l0;  // body-local endpoints
+  const float* grest = W.lrest + B.l0;
+  const float* gstiff = W.lstiff + B.l0;
+  const float gx = W.gx, gy = W.gy, h = W.h;
+  DWorld Wb;  // bounds only
+  Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+  const uint32_t T = blockDim.x, t = threadIdx.x;
+  const uint32_t per = 1u << log2per, mask = per - 1u;
+  const uint32_t sp_a = smem_addr(lsm), sq_a = sp_a + 8u * per;
+  // this CTA's slice of the body: particles [j0, j1)
+  const uint32_t j0 = rank << log2per, j1 = min(B.np, j0 + per);
+  for (uint32_t j = j0 + t; j < j1; j += T) {
+    const uint32_t k = B.first != NO_FIRST ? B.first + j : bidx[j];
+    sts_f32x2(sp_a + 8u * (j - j0), gp[k]);
+    if (FULL) sts_f32x2(sq_a + 8u * (j - j0), gq[k]);
+  }
+  if (CLUSTER) cluster_barrier(); else __syncthreads();
+  auto ld = [&](uint32_t base, uint32_t j) {
+    const uint32_t a = base + 8u * (j & mask);
+    return CLUSTER ? ldc_f32x2(dsmem_addr(a, j >> log2per)) : lds_f32x2(a);
+  };
+  auto st = [&](uint32_t base, uint32_t j, float2 v) {
+    const uint32_t a = base + 8u * (j & mask);
+    if (CLUSTER) stc_f32x2(dsmem_addr(a, j >> log2per), v); else sts_f32x2(a, v);
+  };
+  auto run = [&](uint2 op) {
+    if (FULL && op.y == OP_INTEG) {  // bounds + integrate, src/solver.rs:155-158, :118-121
+      float2 p = ld(sp_a, op.x), q = ld(sq_a, op.x);
+      solve_bounds(p, q, Wb);
+      integrate(p, q, gx, gy, h);
+      st(sp_a, op.x, p);
+      st(sq_a, op.x, q);
+    } else {  // ParticleLink::solve, src/link.rs:18-27
+      uint32_t ia, ib, kl;
+      if (op.y == OP_WIDE) {
+        kl = op.x;
+        const uint2 e = __ldg(gab + kl);
+        ia = e.x;
+        ib = e.y;
+      } else {
+        kl = op.y;
+        ia = op.x & 0xFFFFu;
+        ib = op.x >> 16;
+      }
+      const float rest = __ldg(grest + kl), stiff = __ldg(gstiff + kl);
+      float2 pa = ld(sp_a, ia), pb = ld(sp_a, ib);
+      link_solve(pa, pb, rest, stiff);
+      st(sp_a, ia, pa);
+      st(sp_a, ib, pb);
+    }
+  };
+  const uint32_t g = rank * T + t, CT = C * T;
+  for (uint32_t c = 0; c < S.nchunks; ++c) {
+    const uint32_t* ch = SC.stream + __ldg(SC.chunk_off + S.chunk0 + c);
+    const uint32_t nseg = __ldg(ch);
+    const uint2* ops = reinterpret_cast<const uint2*>(ch + ((2u + nseg) & ~1u));
+    uint32_t beg = 0;
+    for (uint32_t sg = 0; sg < nseg; ++sg) {
+      const uint32_t end = __ldg(ch + 1u + sg);
+      for (uint32_t k = beg + g; k < end; k += CT) run(__ldg(ops + k));
+      if (CLUSTER) cluster_barrier(); else __syncthreads();
+      beg = end;
+    }
+  }
+  // every remote access happened before the last barrier: store the slice
+  for (uint32_t j = j0 + t; j < j1; j += T) {
+    const uint32_t k = B.first != NO_FIRST ? B.first + j : bidx[j];
+    gp[k] = lds_f32x2(sp_a + 8u * (j - j0));
+    if (FULL) gq[k] = lds_f32x2(sq_a + 8u * (j - j0));
+  }
+}
+
+// ----------------------------------------------------------------------------
 // Serial executor: one thread replays one body's reference loops directly, in
 // insertion order (src/solver.rs:143-146, :155-158, :118-121).  Used for
 // chain-like bodies (rings, ropes) whose level schedule has width ~1, where a

@@ -43,6 +43,7 @@ bool PlanTuning::set(const std::string& k, double v) {
   else if (k == "stage_frac") stage_frac = (float)v;
   else if (k == "bucket_factor") bucket_factor = (float)v;
   else if (k == "collide_thread_min") collide_thread_min = (uint32_t)v;
+  else if (k == "large_max") large_max = (uint32_t)v;
   else return false;
   return true;
 }
@@ -203,6 +204,9 @@ static bool check_image(const WorldImage& im, const SchedRegistry& reg, std::str
         (size_t)S.off + S.words > reg.stream.size())
       return bad("schedule range");
     if (g.smem && (!B.local || B.np > 65535u)) return bad("shared-memory body needs local links");
+    if (g.large_c && (g.smem || !B.local || g.large_c > 16u || g.log2per > 14u ||
+                      (size_t)g.large_c << g.log2per < B.np || g.T > 1024u))
+      return bad("large-body executor layout");
     if (g.res && (!g.smem || g.res != S.words * 4u)) return bad("resident schedule size");
     if (g.T < 32 || g.T % 32) return bad("group size");
   }
@@ -370,16 +374,40 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
       if (region + sb + GROUP_TAIL_BYTES <= tune.res_max)
         res = (uint32_t)sb;
     }
-    B.local = smem ? 1u : 0u;
+    // A body over one CTA's shared memory: the large-body executor keeps its
+    // positions (and prev) in the shared memory of a cluster of up to
+    // large_max CTAs, at most 128 KB each (8,192 particles whole-step,
+    // 16,384 for link passes), with link parameters and schedule read
+    // through the caches; beyond that the group executor runs it from
+    // global memory.
+    uint32_t large_c = 0, log2per = 0, TL = T;
+    if (!smem && tune.large_max > 0 && B.np > 0) {
+      const uint32_t cap_log2 = full ? 13u : 14u;
+      uint32_t l2 = 0;
+      while (l2 < cap_log2 && (1u << l2) < B.np) ++l2;
+      const uint32_t c = (B.np + (1u << l2) - 1u) >> l2;
+      if (c <= tune.large_max) {
+        large_c = c;
+        log2per = l2;
+        const float w = avg / (tune.width_per_thread * (float)c);
+        TL = std::min<uint32_t>(1024u, std::max<uint32_t>(64u, pow2ceil((uint32_t)(w + 0.999f))));
+      }
+    }
+    const bool local = smem || large_c > 0;
+    B.local = local ? 1u : 0u;
     for (size_t i = 0; i < loc.size(); ++i) {
-      if (smem) im.lab.push_back(loc[i]);
+      if (local) im.lab.push_back(loc[i]);
       else im.lab.push_back(make_uint2(im.bidx[B.i0 + loc[i].x], im.bidx[B.i0 + loc[i].y]));
     }
     const uint32_t id = (uint32_t)im.bodies.size();
     im.bodies.push_back(B);
-    im.groups.push_back(GroupBody{id, T, smem ? (uint32_t)region : 0u, res, smem});
+    GroupBody gbody{id, large_c ? TL : T, smem ? (uint32_t)region : 0u, res, smem};
+    gbody.large_c = large_c;
+    gbody.log2per = log2per;
+    im.groups.push_back(gbody);
     im.stats.group_bodies++;
-    if (!smem) im.stats.global_bodies++;
+    if (large_c) im.stats.large_bodies++;
+    else if (!smem) im.stats.global_bodies++;
     im.stats.levels += S.nlvl;
     im.stats.ops += S.nops;
   };

@@ -78,6 +78,7 @@ pub struct b2d_plan_stats {
     pub ops: u64,
     pub colours: u32,
     pub device_bytes: u64,
+    pub large_bodies: u32,
 }
 
 #[repr(C)]

@@ -110,7 +110,7 @@ int b2d_set_circle_static(b2d_solver* s, size_t index, int is_static);
 /* executor tunables (the autotuner sets these): serial_width, t_min, t_max,
  * pack_np, pack_nl, free_chunk, smem_max, warp_groups, max_groups,
  * width_per_thread, resident, res_max, stage_frac, bucket_factor,
- * collide_thread_min; they move
+ * collide_thread_min, large_max; they move
  * work between executors and never change results; take effect at the next
  * update; B2D_ERR_ARG for an unknown key */
 int b2d_set_tuning(b2d_solver* s, const char* key, double value);
@@ -177,6 +177,10 @@ typedef struct {
   uint64_t levels, ops;
   uint32_t colours;
   uint64_t device_bytes;
+  /* group bodies over one CTA's shared memory that the large-body executor
+   * runs from the shared memory of a thread-block cluster (global_bodies
+   * counts the ones run from global memory) */
+  uint32_t large_bodies;
 } b2d_plan_stats;
 int b2d_get_plan_stats(b2d_solver* s, b2d_plan_stats* out);
 /* fast mode: the link order actually executed (world link ids) */

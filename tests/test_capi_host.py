@@ -177,7 +177,9 @@ def test_plan_config2_links_only_levels(native_lib):
 
 def test_tunables_move_bodies_between_executors(native_lib):
     """serial_width decides group vs serial execution; smem_max pushes bodies
-    to the global-memory executor; the plan still covers every link."""
+    out of one CTA's shared memory, to the large-body (cluster) executor, or
+    with large_max = 0 to the global-memory executor; the plan still covers
+    every link."""
     from bendy2d_gb300 import scenes
     sc = scenes.config2(seed=1, n_bodies=3, box=100.0, n_circles=1, n_polys=1)
     s = sc.to_solver()
@@ -188,9 +190,14 @@ def test_tunables_move_bodies_between_executors(native_lib):
     assert ser["group_bodies"] == 0
     s2 = sc.to_solver()
     s2.set_tuning(smem_max=1024)
-    glob = s2.plan_stats()
+    large = s2.plan_stats()
+    assert large["large_bodies"] == large["group_bodies"] == base["group_bodies"]
+    assert large["global_bodies"] == 0 and large["ops"] == base["ops"]
+    s3 = sc.to_solver()
+    s3.set_tuning(smem_max=1024, large_max=0)
+    glob = s3.plan_stats()
     assert glob["global_bodies"] == glob["group_bodies"] == base["group_bodies"]
-    assert glob["ops"] == base["ops"]
+    assert glob["large_bodies"] == 0 and glob["ops"] == base["ops"]
 
 
 def test_unknown_tunable_is_rejected(native_lib):

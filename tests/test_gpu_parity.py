@@ -166,16 +166,47 @@ def test_rings_serial_executor_with_stiffness(gpu):
     check(sc, 5, "rings")
 
 
-def test_large_body_runs_from_global_memory(gpu):
-    """A 72x72 cloth does not fit one CTA's shared memory: global executor."""
+def _big_cloth(side, collide, sub_steps, link_iters, seed=2, box=100.0):
     from bendy2d_gb300 import scenes
-    rng = np.random.default_rng(2)
-    body = scenes.grid_body(72, 72, (10.0, 20.0), 1.0, 0.01, rng)
-    sc = scenes._assemble("big", [body], bounds=(0.0, 0.0, 100.0, 100.0), sub_steps=2,
-                          link_iters=2)
+    rng = np.random.default_rng(seed)
+    body = scenes.grid_body(side, side, (10.0, 20.0), 1.0, 0.01, rng)
+    sc = scenes._assemble("big", [body], bounds=(0.0, 0.0, box, box), sub_steps=sub_steps,
+                          link_iters=link_iters, collide=collide)
+    sc.prev = scenes._velocity_prev(sc.pos, rng, 0.5, sc.dt / sub_steps)
+    return sc
+
+
+@pytest.mark.parametrize("side,collide,clusters", [(72, 0, 1), (100, 0, 2), (100, 1, 1)])
+def test_large_body_executor_matches_oracle_and_global_executor(gpu, side, collide, clusters):
+    """A body whose state, links and schedule do not fit one CTA's shared
+    memory: the large-body executor (positions in the shared memory of a
+    cluster of `clusters` CTAs) and, with large_max = 0, the global-memory
+    group executor both match the oracle bit for bit."""
+    from oracle import load_scene
+    sc = _big_cloth(side, collide, 2, 2)
     s = sc.to_solver()
-    assert s.plan_stats()["global_bodies"] == 1
-    check(sc, 3, "global executor")
+    st = s.plan_stats()
+    assert st["large_bodies"] == 1 and st["global_bodies"] == 0
+    g = sc.to_solver()
+    g.set_tuning(large_max=0)
+    assert g.plan_stats()["global_bodies"] == 1
+    o = load_scene(sc)
+    for _ in range(3):
+        s.update(sc.dt)
+        g.update(sc.dt)
+        assert o.update(sc.dt) == 0
+    assert_same_state(solver_state(s), oracle_state(o), f"large-body executor {side}x{side}")
+    assert_same_state(solver_state(g), oracle_state(o), f"global executor {side}x{side}")
+
+
+def test_large_body_cluster_with_wide_ops(gpu):
+    """A 260x260 cloth (67,600 particles) with particle collisions: its link
+    passes run on a cluster of five CTAs, with link endpoints read from the
+    body-local link table (more than 65,535 particles)."""
+    sc = _big_cloth(260, 1, 2, 1, seed=5, box=300.0)
+    s = sc.to_solver()
+    assert s.plan_stats()["large_bodies"] == 1
+    check(sc, 2, "cluster of five CTAs")
 
 
 def test_free_particles_and_mixed_components(gpu):

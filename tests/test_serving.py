@@ -53,8 +53,8 @@ def _oracle_after(world, steps):
 
 def _big_world():
     """A configuration-4-style request whose 100x100 cloth (10,000 particles,
-    39,402 links) does not fit one CTA's shared memory even for the link
-    passes alone (global-memory executor), with particle collisions."""
+    39,402 links) does not fit one CTA's shared memory with its links and
+    schedule (large-body executor), with particle collisions."""
     from bendy2d_gb300 import scenes
     from bendy2d_gb300.scenes import COLLIDE_PP
     rng = np.random.default_rng(21)
@@ -72,7 +72,7 @@ def test_served_results_match_oracle_alone_and_in_mix(gpu):
     from bendy2d_gb300.serving import Server
     pool = _pool(24, seed=31, lo=64, hi=3000)
     big = _big_world()
-    assert big.to_solver().plan_stats()["global_bodies"] == 1
+    assert big.to_solver().plan_stats()["large_bodies"] == 1
     items = [(w, 2 + (i * 5) % 7) for i, w in enumerate(pool)] + [(big, 3)]
     sv = Server(1 << 33)
     sv.start()
