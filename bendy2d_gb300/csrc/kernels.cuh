@@ -757,6 +757,20 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
         sab[sb.y + i] = W.lab[B.l0 + i];  // body-local endpoints
         srs[sb.y + i] = make_float2(W.lrest[B.l0 + i], W.lstiff[B.l0 + i]);
       }
+    } else {
+      // the chain reads each link's data one link ahead, which hides an L2
+      // hit but not a DRAM access: bring the body's link arrays into L2
+      // now, one prefetch per 128-byte line (endpoints 8 B, rest and
+      // stiffness 4 B a link)
+      const char* ab = reinterpret_cast<const char*>(W.lab + B.l0);
+      const char* rs = reinterpret_cast<const char*>(W.lrest + B.l0);
+      const char* sf = reinterpret_cast<const char*>(W.lstiff + B.l0);
+      for (uint32_t o = 128u * lane; o < 8u * B.nl; o += 32u * 128u)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(ab + o));
+      for (uint32_t o = 128u * lane; o < 4u * B.nl; o += 32u * 128u) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(rs + o));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(sf + o));
+      }
     }
   }
   __syncthreads();
