@@ -514,9 +514,33 @@ def kernel_rooflines(prof: dict, sc, launches_per_step: dict) -> dict:
     return out
 
 
+# Warp-instructions per link solve of the shared-memory link executor, from
+# its ncu captures (instructions executed / link solves of the launch):
+# configuration 5, 133.4 M / 32.0 M (profiles/config5_collide_and_links.md);
+# configuration 2, 4.34 M / 1.0 M (profiles/exec_groups_links_config2.md).
+LINK_WARP_INSTR = {"config5": 133.4e6 / (1024 * 3906 * 8), "config2": 4.3354e6 / (64 * 3906 * 4)}
+
+
+def link_issue_bound(torch, ms_per_step: float, solves_per_step: float, per_solve: float) -> dict:
+    """The link executor against the SMs' instruction-issue rate (one
+    warp-instruction per cycle per sub-partition, four per SM, at the
+    maximum SM clock): link solves x warp-instructions per solve / time."""
+    props = torch.cuda.get_device_properties(0)
+    mhz = 2070.0
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        mhz = float(json.loads(p.read_text()).get("sm_max_mhz", mhz))
+    peak = props.multi_processor_count * 4 * mhz * 1e6
+    achieved = solves_per_step * per_solve / (ms_per_step / 1e3)
+    return {"bound": "issue", "warp_instructions_per_link_solve": per_solve,
+            "achieved": achieved, "peak": peak, "unit": "warp-instructions/s",
+            "frac": achieved / peak}
+
+
 def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
     """Per-kernel rooflines of one configuration-5 update at this
-    throughput-bound size (kernel_rooflines)."""
+    throughput-bound size (kernel_rooflines), with the link executor also
+    against the instruction-issue rate, its real bound here."""
     with torch.cuda.stream(stream):
         flush.zero_()
     s.synchronize()
@@ -525,9 +549,14 @@ def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
     prof = s.profile()
     s.set_profiling(False)
     S = sc.sub_steps
-    return kernel_rooflines(prof, sc, {"links": S, "grid_count": S, "grid_scan": S,
-                                       "grid_scatter": S, "collide_integrate": S,
-                                       "rigid": S + 1, "copy_back": 1})
+    out = kernel_rooflines(prof, sc, {"links": S, "grid_count": S, "grid_scan": S,
+                                      "grid_scatter": S, "collide_integrate": S,
+                                      "rigid": S + 1, "copy_back": 1})
+    if "links" in out:
+        out["links"]["issue"] = link_issue_bound(
+            torch, out["links"]["ms_per_step"], S * sc.link_iters * len(sc.la),
+            LINK_WARP_INSTR["config5"])
+    return out
 
 
 def overlap_at_start(sc):
@@ -783,7 +812,9 @@ def main():
     if dom.startswith("exec_groups"):
         st = s.plan_stats()
         lv = st["levels"] / max(1, st["group_bodies"])
-        chain = {"levels_per_launch": lv, "ns_per_level": dom_ms * 1e6 / lv}
+        chain = {"levels_per_launch": lv, "ns_per_level": dom_ms * 1e6 / lv,
+                 "issue": link_issue_bound(torch, dom_ms, sc.link_iters * len(sc.la),
+                                           LINK_WARP_INSTR["config2"])}
 
     # every rank steps its shard of the configuration-3 worlds
     batched = None
