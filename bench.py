@@ -595,7 +595,14 @@ def run_profile_config(args, torch) -> None:
     b.build()
     torch.cuda.set_device(0)
     k = args.profile_config
-    if k == 1:
+    if args.profile_large:
+        n = args.profile_large
+        rng = np.random.default_rng(0)
+        sc = scenes._assemble(f"cloth{n}", [scenes.grid_body(n, n, (10.0, 20.0), 1.0, 0.01, rng)],
+                              bounds=(0.0, 0.0, 4.0 * n, 4.0 * n), sub_steps=8, link_iters=4)
+        runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
+        k = f"large{n}"
+    elif k == 1:
         sc = scenes.config1(seed=0)
         runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
     elif k == 2:
@@ -664,6 +671,10 @@ def main():
     ap.add_argument("--profile-config", type=int, choices=[1, 2, 3, 5], default=0,
                     help="run only --warmup + --steps updates of one configuration (the "
                          "command the ncu summaries profile) and print its step time")
+    ap.add_argument("--profile-large", type=int, default=0, metavar="SIDE",
+                    help="like --profile-config, for one SIDE x SIDE cloth without "
+                         "collisions (8 sub-steps, 4 link passes): a body for the "
+                         "large-body executor when it exceeds one CTA's shared memory")
     args = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -702,7 +713,7 @@ def main():
         return
 
     import torch
-    if args.profile_config:
+    if args.profile_config or args.profile_large:
         run_profile_config(args, torch)
         return
     if world > 1:
