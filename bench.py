@@ -457,9 +457,19 @@ def grid_buckets(sc) -> int:
     return 1 << (n - 1).bit_length()
 
 
-def kernel_byte_models(sc) -> dict:
+# the engine's default for the tunable grid_slot_max: collision grids of up
+# to this many particles are built by slot inserts, larger ones by a sort
+GRID_SLOT_MAX = 262144
+
+
+def kernel_byte_models(sc, slotted=None) -> dict:
     """Algorithmic bytes per launch of every kernel of the sub-step pipeline,
-    each array counted once (f32 state, u32 indices).  name -> (bytes, model)."""
+    each array counted once (f32 state, u32 indices).  name -> (bytes, model).
+    slotted: the collision grid is built by slot inserts, else by the
+    counting sort (count, scan, scatter); None: the engine's default choice
+    for this world's size."""
+    if slotted is None:
+        slotted = sc.n_particles <= GRID_SLOT_MAX
     n, l, I = sc.n_particles, len(sc.la), sc.link_iters
     nb = grid_buckets(sc)
     nv = sum(len(g["points"]) for g in sc.polygons)
@@ -475,11 +485,18 @@ def kernel_byte_models(sc) -> dict:
         "grid_scan": (16.0 * nb, "per bucket: read count 4 B, clear it 4 B, write range 8 B"),
         "grid_scatter": (40.0 * n, "per particle: read pos 8 B, (bucket, rank) 8 B, range 8 B, "
                                    "write sorted entry 16 B"),
-        "collide_integrate": (56.0 * n + 8.0 * nb,
-                              "per particle: pos and prev read, pos and prev written (32 B), "
-                              "its sorted entry read (16 B), its (bucket, rank) slot 8 B; per "
-                              "bucket its range once (8 B); neighbour entries re-read through "
-                              "L1/L2 are not counted again"),
+        "grid_insert": (32.0 * n, "per particle: read pos 8 B, bucket cell word atomic 8 B, "
+                                  "write its entry 16 B (a slot or an overflow entry)"),
+        "collide_integrate": ((48.0 * n + 16.0 * nb,
+                               "per particle: pos and prev read, pos and prev written (32 B), "
+                               "its entry read (16 B); per bucket its cell word read once (8 B) "
+                               "and the other parity's cleared (8 B); neighbour entries re-read "
+                               "through L1/L2 are not counted again") if slotted else
+                              (56.0 * n + 8.0 * nb,
+                               "per particle: pos and prev read, pos and prev written (32 B), "
+                               "its sorted entry read (16 B), its (bucket, rank) slot 8 B; per "
+                               "bucket its range once (8 B); neighbour entries re-read through "
+                               "L1/L2 are not counted again")),
         "rigid": (48.0 * (nc + nv), "per circle and polygon vertex: pos, prev, acc read and "
                                     "written"),
         "copy_back": (16.0 * n, "per particle: read pos from the second buffer, write it back"),
@@ -492,10 +509,11 @@ def kernel_rooflines(prof: dict, sc, launches_per_step: dict) -> dict:
     (kernel_byte_models) / mean launch time, against the measured HBM copy
     bandwidth.  The times of all kernels add up to the serial step time."""
     peak, kind = _peaks()
-    models = kernel_byte_models(sc)
+    models = kernel_byte_models(sc, slotted="grid_scan" not in prof)
     groups = {"links": [k for k in prof if k.startswith("exec_")],
               "rigid": [k for k in prof if k.startswith("rigid")]}
-    for k in ("grid_count", "grid_scan", "grid_scatter", "collide_integrate", "copy_back"):
+    for k in ("grid_insert", "grid_count", "grid_scan", "grid_scatter", "collide_integrate",
+              "copy_back"):
         groups[k] = [k] if k in prof else []
     out = {}
     for g, names in groups.items():
@@ -549,9 +567,9 @@ def config5_kernel_rooflines(s, sc, torch, flush, stream) -> dict:
     prof = s.profile()
     s.set_profiling(False)
     S = sc.sub_steps
-    out = kernel_rooflines(prof, sc, {"links": S, "grid_count": S, "grid_scan": S,
-                                      "grid_scatter": S, "collide_integrate": S,
-                                      "rigid": S + 1, "copy_back": 1})
+    out = kernel_rooflines(prof, sc, {"links": S, "grid_insert": S, "grid_count": S,
+                                      "grid_scan": S, "grid_scatter": S,
+                                      "collide_integrate": S, "rigid": S + 1, "copy_back": 1})
     if "links" in out:
         out["links"]["issue"] = link_issue_bound(
             torch, out["links"]["ms_per_step"], S * sc.link_iters * len(sc.la),
@@ -802,7 +820,8 @@ def main():
     def launches_per_step(name: str) -> int:
         if name.startswith("exec_") and "full" not in name:
             return sc.sub_steps  # one link-phase launch per sub-step
-        if name in ("grid_count", "grid_scan", "grid_scatter", "collide_integrate"):
+        if name in ("grid_insert", "grid_count", "grid_scan", "grid_scatter",
+                    "collide_integrate"):
             return sc.sub_steps
         if name == "rigid_ext":
             return sc.sub_steps + 1  # phase A of sub-step 0, B+A between sub-steps, B last
@@ -886,7 +905,8 @@ def main():
         "kernel_ms_per_step": {k: v / nprof for k, v in sorted(prof_tot.items())},
         "kernel_rooflines": kernel_rooflines(
             {k: v / nprof for k, v in prof_tot.items()}, sc,
-            {"links": sc.sub_steps, "grid_count": sc.sub_steps, "grid_scan": sc.sub_steps,
+            {"links": sc.sub_steps, "grid_insert": sc.sub_steps, "grid_count": sc.sub_steps,
+             "grid_scan": sc.sub_steps,
              "grid_scatter": sc.sub_steps, "collide_integrate": sc.sub_steps,
              "rigid": sc.sub_steps + 1, "copy_back": 1}),
         "gpu_launches": launches,

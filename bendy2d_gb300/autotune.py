@@ -14,6 +14,8 @@ updates after warm-up) and the fastest kept.  Tunables:
   bucket_factor     collision-grid buckets per world: pow2 >= this x particles
   collide_thread_min  particles in the collide pass from which it runs one
                     thread per particle instead of three lanes each
+  grid_slot_max     collision particles up to which the grid is built by
+                    slot inserts (above: a counting sort each sub-step)
 The tuning only moves work between executors and launch shapes; results are
 bit-identical whatever it picks.  Results are cached in memory by a scene
 signature.
@@ -31,6 +33,7 @@ SPACE = {
     "stage_frac": [0.4, 0.67, 1.01],
     "bucket_factor": [1.0, 2.0, 4.0],
     "collide_thread_min": [0, 131072, 1 << 30],
+    "grid_slot_max": [0, 262144, 1 << 30],
 }
 # The planner's defaults for the tunables above (PlanTuning in
 # csrc/engine.hpp); a candidate is always applied on top of these, so one
@@ -44,6 +47,7 @@ DEFAULTS = {
     "stage_frac": 0.67,
     "bucket_factor": 2.0,
     "collide_thread_min": 131072,
+    "grid_slot_max": 262144,
 }
 # tunables that matter for batches of chain-like worlds (rings), where the
 # serial executors carry the step

@@ -21,8 +21,9 @@ namespace b2d {
 enum : uint32_t { COLLIDE_PP = 1u, COLLIDE_PC = 2u, COLLIDE_PPOLY = 4u };
 // World flag set by the planner: every solver particle of this world belongs
 // to a body that the shared-memory link executor runs, so that executor
-// enters each particle into the collision grid's counting pass as it stores
-// the body back (no separate count kernel for this world).
+// enters each particle into the collision grid (a slot insert, or the
+// sorted grid's count) as it stores the body back: no separate insert or
+// count kernel for this world.
 constexpr uint32_t GRID_IN_LINKS = 8u;
 
 // Schedule op encoding: link ops carry the body-local link index; bounds +
@@ -154,6 +155,26 @@ struct DGrid {
   uint32_t* cursor;      // entries of sorted handed out so far this sub-step
   uint2* pbr;            // per particle: (bucket, rank within bucket)
   uint4* sorted;         // cap entries: {pos.x bits, pos.y bits, cell x, cell y}
+  uint32_t* err;         // device error word (ERR_BIT_*)
+  uint32_t nbuckets;
+  uint32_t cap;
+};
+
+// The engine's form of the same grid: no sort.  Each particle is inserted
+// straight into its bucket, whose first GRID_SLOTS entries sit in fixed
+// slots; later ones go to an overflow array, chained per bucket.  A
+// sub-step's inserts use the cell words of parity sub & 1; that sub-step's
+// collide pass clears the other parity's words for the next sub-step (and
+// resets the overflow cursor).  Slots are interleaved by strip (four
+// buckets): slot k of the strip's four buckets is one 64-byte run, so the
+// first entries of a row of neighbour cells share a cache line.
+constexpr uint32_t GRID_SLOTS = 4;
+struct DSlots {
+  uint2* cell;           // 2 x nbuckets (parity-major): {entries, overflow head + 1 (0: none)}
+  uint4* slot;           // nbuckets x GRID_SLOTS entries {pos.x bits, pos.y bits, cell x, cell y}
+  uint4* ovf;            // cap overflow entries
+  uint32_t* ovf_next;    // cap: the bucket's next overflow entry + 1 (0: end)
+  uint32_t* cursor;      // overflow entries handed out this sub-step
   uint32_t* err;         // device error word (ERR_BIT_*)
   uint32_t nbuckets;
   uint32_t cap;

@@ -407,29 +407,69 @@ int Engine::check_device_error() {
 }
 
 int Engine::ensure_grid(size_t nbuckets, size_t np_pp) {
-  if (nbuckets <= grid_.nbuckets && np_pp <= grid_np_ && d_grid_) return OK;
+  // Slot inserts skip the scan and scatter launches but spread the entries
+  // over GRID_SLOTS fixed slots per bucket: on GB300 that wins up to a few
+  // hundred thousand particles (65,536 scattered cloth particles: 0.544 ->
+  // 0.518 ms per update; 131,072: 0.728 -> 0.579), while for a million
+  // particles packed on a lattice the sparse slots cost the collide pass
+  // more than the two launches (5.91 -> 6.28 ms).
+  // (A grid in one form keeps it until the particle count is well past the
+  // threshold, so that a serving pool near it does not reallocate each step.)
+  const uint64_t lim = tune_.grid_slot_max;
+  const bool slotted = !d_grid_ ? np_pp <= lim
+                       : grid_slotted_ ? np_pp <= lim
+                                       : (uint64_t)np_pp * 2 <= lim;
+  if (nbuckets <= grid_.nbuckets && np_pp <= grid_np_ && d_grid_ && slotted == grid_slotted_)
+    return OK;
   const size_t nb = std::max(nbuckets, (size_t)grid_.nbuckets);
   const size_t np = std::max<size_t>(std::max(np_pp, grid_np_), 1);
   size_t bytes = 0;
   auto seg = [&](size_t b) { size_t at = bytes; bytes = (bytes + b + 255) & ~(size_t)255; return at; };
-  const size_t o_count = seg(nb * 4), o_start = seg(nb * 8), o_cursor = seg(4),
-               o_pbr = seg(np * 8), o_sorted = seg(np * 16);
+  size_t o[5];
+  if (slotted) {  // cell words (2 parities), cursor | slots, overflow entries, overflow links
+    o[0] = seg(nb * 16);
+    o[1] = seg(4);
+    o[2] = seg(nb * GRID_SLOTS * 16);
+    o[3] = seg(np * 16);
+    o[4] = seg(np * 4);
+  } else {        // counts, ranges, cursor | (bucket, rank) per particle, sorted entries
+    o[0] = seg(nb * 4);
+    o[1] = seg(nb * 8);
+    o[2] = seg(4);
+    o[3] = seg(np * 8);
+    o[4] = seg(np * 16);
+  }
   B2D_CUDA(cudaStreamSynchronize(stream_));
   if (d_grid_) dev_bytes_ -= grid_bytes_;
   cudaFree(d_grid_);
   d_grid_ = nullptr;
+  grid_ = DGrid{};
+  gslots_ = DSlots{};
   B2D_CUDA(cudaMalloc(&d_grid_, bytes));
   B2D_CUDA(cudaMemset(d_grid_, 0, bytes));
-  grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o_count);
-  grid_.range = reinterpret_cast<uint2*>(d_grid_ + o_start);
-  grid_.cursor = reinterpret_cast<uint32_t*>(d_grid_ + o_cursor);
-  grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o_pbr);
-  grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o_sorted);
+  if (slotted) {
+    gslots_.cell = reinterpret_cast<uint2*>(d_grid_ + o[0]);
+    gslots_.cursor = reinterpret_cast<uint32_t*>(d_grid_ + o[1]);
+    gslots_.slot = reinterpret_cast<uint4*>(d_grid_ + o[2]);
+    gslots_.ovf = reinterpret_cast<uint4*>(d_grid_ + o[3]);
+    gslots_.ovf_next = reinterpret_cast<uint32_t*>(d_grid_ + o[4]);
+    gslots_.nbuckets = (uint32_t)nb;
+    gslots_.cap = (uint32_t)np;
+    grid_head_bytes_ = o[2];
+  } else {
+    grid_.count = reinterpret_cast<uint32_t*>(d_grid_ + o[0]);
+    grid_.range = reinterpret_cast<uint2*>(d_grid_ + o[1]);
+    grid_.cursor = reinterpret_cast<uint32_t*>(d_grid_ + o[2]);
+    grid_.pbr = reinterpret_cast<uint2*>(d_grid_ + o[3]);
+    grid_.sorted = reinterpret_cast<uint4*>(d_grid_ + o[4]);
+    grid_head_bytes_ = o[3];
+  }
+  // the bucket count (both forms) is read back through grid_.nbuckets
   grid_.nbuckets = (uint32_t)nb;
   grid_.cap = (uint32_t)np;
+  grid_slotted_ = slotted;
   grid_np_ = np;
   grid_bytes_ = bytes;
-  grid_head_bytes_ = o_pbr;
   grid_reset_ = false;
   dev_bytes_ += bytes;
   invalidate_graph();
@@ -759,8 +799,13 @@ int Engine::launch_all(bool profiling) {
   };
   const DScheds SC{d_scheds_, d_chunk_off_, d_chunk_len_, d_stream_, d_err_, fault_bits_};
   grid_.err = d_err_;
-  DGrid GR = grid_;  // as launched: the capacity may be lowered by FAULT_GRID_CAP
+  gslots_.err = d_err_;
+  // as launched: the capacity (sorted entries, or overflow entries of the
+  // slotted grid) may be lowered by FAULT_GRID_CAP
+  DGrid GR = grid_;
+  DSlots GS = gslots_;
   if (fault_grid_cap_ && fault_grid_cap_ < GR.cap) GR.cap = fault_grid_cap_;
+  if (fault_grid_cap_ && fault_grid_cap_ < GS.cap) GS.cap = fault_grid_cap_;
   const DWorld* W = d_worlds_;
   // Streams: link executors, grid and collide kernels run on the main
   // stream; circle/polygon kernels on aux streams (graph branches), joined
@@ -840,12 +885,12 @@ int Engine::launch_all(bool profiling) {
     // filled every SM and delayed that branch: 18 % slower on 1,024 bodies.)
     const bool pdl = !profiling && !c.full && c.res && st == stream_;
     void (*k)(const DWorld*, DScheds, const uint2*, uint32_t, uint32_t, uint32_t, uint32_t,
-              uint32_t, uint32_t, uint32_t, uint32_t*, uint2*) =
+              uint32_t, uint32_t, uint32_t, uint32_t*, uint2*, DSlots) =
         c.res ? (c.full ? k_exec_groups<true, true, true> : k_exec_groups<false, true, true>)
         : c.full ? (c.smem ? k_exec_groups<true, true, false> : k_exec_groups<true, false, false>)
                  : (c.smem ? k_exec_groups<false, true, false> : k_exec_groups<false, false, false>);
     lk(launch_k(k, grid, block, sm, st, pdl, W, SC, L, n, c.T, c.G, rg, sb, cur, sub, GR.count,
-                GR.pbr));
+                GR.pbr, GS));
   };
   auto groups = [&](bool full, uint32_t cur, uint32_t sub) {
     for (const LaunchClass& c : classes_) {
@@ -966,7 +1011,16 @@ int Engine::launch_all(bool profiling) {
       });
     }
     end_pass();
-    if (any_pp_) {
+    if (any_pp_ && grid_slotted_) {
+      // the cell words of this parity are all zero here (cleared by the
+      // previous sub-step's collide pass, or by k_copy_back); worlds whose
+      // link executor inserted their particles skip the insert pass
+      if (any_count_)
+        timed("grid_insert", [&] {
+          lk(launch_k(k_grid_insert, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GS, CH,
+                      nch, cur, s));
+        });
+    } else if (any_pp_) {
       // counts are all zero here: the scan of the previous sub-step cleared them.
       // Small grids: one 256-thread CTA per 1,024-bucket tile; large ones:
       // 16,384-bucket tiles over at most one 1024-thread CTA per SM.
@@ -995,12 +1049,21 @@ int Engine::launch_all(bool profiling) {
     }
     if (nre) edge(ax, stream_);
     timed("collide_integrate", [&] {
-      if (collide_per_particle_)
-        lk(launch_k(k_collide_particle, dim3(nch), dim3(COLLIDE_P_THREADS), 0, stream_,
-                    !profiling, W, GR, CH, nch, cur, s));
-      else
-        lk(launch_k(k_collide_integrate, dim3(nch * COLLIDE_CTAS), dim3(COLLIDE_THREADS), 0,
-                    stream_, !profiling, W, GR, CH, nch, cur, s));
+      if (grid_slotted_ || !any_pp_) {
+        if (collide_per_particle_)
+          lk(launch_k(k_collide_particle<DSlots>, dim3(nch), dim3(COLLIDE_P_THREADS), 0, stream_,
+                      !profiling, W, GS, CH, nch, cur, s));
+        else
+          lk(launch_k(k_collide_integrate<DSlots>, dim3(nch * COLLIDE_CTAS),
+                      dim3(COLLIDE_THREADS), 0, stream_, !profiling, W, GS, CH, nch, cur, s));
+      } else {
+        if (collide_per_particle_)
+          lk(launch_k(k_collide_particle<DGrid>, dim3(nch), dim3(COLLIDE_P_THREADS), 0, stream_,
+                      !profiling, W, GR, CH, nch, cur, s));
+        else
+          lk(launch_k(k_collide_integrate<DGrid>, dim3(nch * COLLIDE_CTAS),
+                      dim3(COLLIDE_THREADS), 0, stream_, !profiling, W, GR, CH, nch, cur, s));
+      }
     });
     if (nre) edge(stream_, ax);
   }
@@ -1009,7 +1072,12 @@ int Engine::launch_all(bool profiling) {
       if (rigid_wide_ext_) k_rigid<2, 1024><<<nre, 1024, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_);
       else k_rigid<2, 256><<<nre, 256, rigid_smem_, ax>>>(W, RE, nre, smax_ext_ - 1, rigid_smem_);
     });
-    timed("copy_back", [&] { k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch); });
+    // an odd sub-step count leaves parity 0's cell words for k_copy_back to clear
+    const bool clear0 = any_pp_ && grid_slotted_ && (smax_ext_ & 1u);
+    timed("copy_back", [&] {
+      k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch, clear0 ? GS.cell : nullptr,
+                                               clear0 ? GS.nbuckets : 0u);
+    });
   }
   edge(ax, stream_);
   edge(ax2, stream_);

@@ -46,6 +46,9 @@ struct PlanTuning {
                                          // one thread per particle (else three lanes each)
   uint32_t large_max = 8;           // largest cluster of the large-body executor (0: bodies
                                     // over one CTA's shared memory run from global memory)
+  uint32_t grid_slot_max = 262144;  // particles in the collision grid up to which it is
+                                    // built by slot inserts; above, by a counting sort per
+                                    // sub-step (count, scan, scatter)
   // set a tunable by name; returns false for an unknown name
   bool set(const std::string& key, double value);
 };
@@ -243,16 +246,21 @@ class Engine {
                    bool allow_large);
   std::vector<WorldLaunch> wlaunch_;
   bool any_pp_ = false;
-  bool any_count_ = false;  // a world with particle collisions needs the count kernel
+  bool any_count_ = false;  // a world with particle collisions needs the insert (count) kernel
   bool collide_per_particle_ = false;  // k_collide_particle instead of k_collide_integrate
   uint32_t rigid_smem_ = 0;
   uint32_t grid_used_ = 0;
   size_t grid_bytes_ = 0;
-  size_t grid_head_bytes_ = 0;  // count, range and scan words at the start of d_grid_
+  // words at the start of d_grid_ that a failed step can leave partial (sorted
+  // grid: counts, ranges, cursor; slotted grid: both parities' cell words and
+  // the overflow cursor)
+  size_t grid_head_bytes_ = 0;
   bool grid_reset_ = false;     // clear them before the next step (after a failure)
   bool lists_dirty_ = true;
-  // broadphase
+  // broadphase: one of the two forms, as allocated
+  bool grid_slotted_ = false;
   DGrid grid_{};
+  DSlots gslots_{};
   size_t grid_np_ = 0;
   unsigned char* d_grid_ = nullptr;
   // graph

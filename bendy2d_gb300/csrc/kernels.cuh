@@ -134,6 +134,32 @@ __device__ __forceinline__ uint32_t bucket_of(const DWorld& W, int32_t cx, int32
   return W.gb0 + (((cell_hash(cx >> 2, cy) << 2) | ((uint32_t)cx & 3u)) & W.gmask);
 }
 
+// Slotted grid (DSlots): slot k of bucket b, interleaved by strip
+__device__ __forceinline__ uint32_t slot_index(uint32_t b, uint32_t k) {
+  return ((b >> 2) * GRID_SLOTS + k) * 4u + (b & 3u);
+}
+// Enter a particle at p in cell (cx, cy), bucket b, into the sub-step's
+// cell words: a fixed slot while the bucket has one free, else the overflow
+// array (refused past its capacity: ERR_BIT_GRID_OVERFLOW, the entry is
+// dropped and the update reports the error).
+__device__ __forceinline__ void grid_insert(const DSlots& G, uint32_t sub, uint32_t b, float2 p,
+                                            int32_t cx, int32_t cy) {
+  uint2* cl = G.cell + (size_t)(sub & 1u) * G.nbuckets + b;
+  const uint4 e = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), (uint32_t)cx, (uint32_t)cy);
+  const uint32_t r = atomicAdd(&cl->x, 1u);
+  if (r < GRID_SLOTS) {
+    G.slot[slot_index(b, r)] = e;
+    return;
+  }
+  const uint32_t o = atomicAdd(G.cursor, 1u);
+  if (o >= G.cap) {
+    atomicOr(G.err, ERR_BIT_GRID_OVERFLOW);
+    return;
+  }
+  G.ovf[o] = e;
+  G.ovf_next[o] = atomicExch(&cl->y, o + 1u);
+}
+
 // Group barrier: a group is one warp (syncwarp) or a named barrier over T
 // threads.  Both order shared and global memory among the group's threads.
 __device__ __forceinline__ void group_sync(uint32_t g, uint32_t T) {
@@ -260,7 +286,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
                               const uint2* __restrict__ list, uint32_t nlist, uint32_t T,
                               uint32_t G, uint32_t region_bytes, uint32_t sched_bytes,
                               uint32_t cur, uint32_t sub, uint32_t* __restrict__ gcount,
-                              uint2* __restrict__ gpbr) {
+                              uint2* __restrict__ gpbr, DSlots GS) {
   extern __shared__ __align__(128) unsigned char smem[];
   pdl_trigger();
   const uint32_t g = threadIdx.x / T, t = threadIdx.x - g * T;
@@ -506,16 +532,18 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
     const float2* sp = reinterpret_cast<const float2*>(base);
     const float2* sq = sp + B.np;
     if (!FULL && (W.flags & GRID_IN_LINKS)) {
-      // store back and enter each particle into the grid's counting pass
-      // (what k_grid_count does for other worlds): its bucket, and its rank
-      // in the bucket from the counter
+      // store back and enter each particle into the grid (what
+      // k_grid_insert / k_grid_count do for other worlds): into its bucket's
+      // slots, or for the sorted grid its bucket and its rank in the bucket
       for (uint32_t i = t; i < B.np; i += T) {
         const uint32_t k = B.first != NO_FIRST ? B.first + i : bidx[i];
         const float2 p = sp[i];
         gp[k] = p;
-        const uint32_t b = bucket_of(W, cell_coord(p.x, W.bx, W.cell, W.icell),
-                                     cell_coord(p.y, W.by, W.cell, W.icell));
-        gpbr[W.gp0 + k] = make_uint2(b, atomicAdd(&gcount[b], 1u));
+        const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell);
+        const int32_t cy = cell_coord(p.y, W.by, W.cell, W.icell);
+        const uint32_t b = bucket_of(W, cx, cy);
+        if (GS.cell != nullptr) grid_insert(GS, sub, b, p, cx, cy);
+        else gpbr[W.gp0 + k] = make_uint2(b, atomicAdd(&gcount[b], 1u));
       }
       return;
     }
@@ -1385,6 +1413,28 @@ static __global__ void __launch_bounds__(CHUNK) k_grid_count(const DWorld* __res
   G.pbr[W.gp0 + j] = make_uint2(b, r);
 }
 
+// The slotted grid's whole build: each particle goes straight into its
+// bucket (worlds whose link executor inserted them are skipped).  The cell
+// words of this sub-step's parity are all zero here: the previous
+// sub-step's collide pass cleared them.
+static __global__ void __launch_bounds__(CHUNK) k_grid_insert(const DWorld* __restrict__ worlds,
+                                                       DSlots G, const uint2* __restrict__ chunks,
+                                                       uint32_t nchunks, uint32_t cur,
+                                                       uint32_t sub) {
+  pdl_trigger();
+  const uint2 ch = chunks[blockIdx.x < nchunks ? blockIdx.x : 0u];
+  const DWorld& W = worlds[ch.x];
+  const uint32_t j = ch.y + threadIdx.x;
+  const bool act = blockIdx.x < nchunks && j < W.np && sub < W.S &&
+                   (W.flags & (COLLIDE_PP | GRID_IN_LINKS)) == COLLIDE_PP;
+  const float2* P = W.pos[cur];
+  pdl_wait();  // positions from the link phase
+  if (!act) return;
+  const float2 p = P[j];
+  const int32_t cx = cell_coord(p.x, W.bx, W.cell, W.icell), cy = cell_coord(p.y, W.by, W.cell, W.icell);
+  grid_insert(G, sub, bucket_of(W, cx, cy), p, cx, cy);
+}
+
 // block-wide exclusive scan of four values per thread at once (THREADS a
 // multiple of 32, at most 1024); the four lanes scan independently.
 // Returns the exclusive prefix of each lane and stores the four block
@@ -1652,6 +1702,58 @@ __device__ __forceinline__ void visit_cell(const DGrid& G, float2 p, int32_t ncx
   }
 }
 
+// The collide kernels over either grid form.  grid_head: what a bucket's
+// walk starts from (its range in `sorted`, or its cell word); grid_visit:
+// the walk of bucket b for cell (ncx, ncy).
+__device__ __forceinline__ uint2 grid_head(const DGrid& G, uint32_t, uint32_t b) {
+  return G.range[b];
+}
+__device__ __forceinline__ uint2 grid_head(const DSlots& G, uint32_t sub, uint32_t b) {
+  return G.cell[(size_t)(sub & 1u) * G.nbuckets + b];
+}
+__device__ __forceinline__ void grid_visit(const DGrid& G, float2 p, int32_t ncx, int32_t ncy,
+                                           uint32_t, uint2 h, float D, float D2, Contacts& c) {
+  visit_cell(G, p, ncx, ncy, h.x, h.y, D, D2, c);
+}
+// Slots first, then the overflow chain (at most cap links: the chain is
+// built acyclic, the bound only keeps a walk finite whatever the words say).
+__device__ __forceinline__ void grid_visit(const DSlots& G, float2 p, int32_t ncx, int32_t ncy,
+                                           uint32_t b, uint2 h, float D, float D2, Contacts& c) {
+  const uint32_t n = h.x < GRID_SLOTS ? h.x : GRID_SLOTS;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint4 e = G.slot[slot_index(b, k)];
+    if (e.z != (uint32_t)ncx || e.w != (uint32_t)ncy) continue;
+    pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, c);
+  }
+  uint32_t o = h.y;
+  for (uint32_t it = 0; o != 0u && o <= G.cap && it < G.cap; ++it) {
+    const uint4 e = G.ovf[o - 1u];
+    o = G.ovf_next[o - 1u];
+    if (e.z != (uint32_t)ncx || e.w != (uint32_t)ncy) continue;
+    pp_contact(p, make_float2(__uint_as_float(e.x), __uint_as_float(e.y)), D, D2, c);
+  }
+}
+// Called by every thread of a collide launch once this sub-step's build is
+// complete.  Sorted grid: the scan is done with the cursor; clear it for the
+// next sub-step's scan.  Slotted grid: reset the overflow cursor and clear
+// the other parity's cell words for the next sub-step's inserts.  Engines
+// without particle collisions have no grid (null pointers) but still run the
+// collide kernels.
+__device__ __forceinline__ void grid_done(const DGrid& G, uint32_t) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && G.cursor != nullptr) *G.cursor = 0u;
+}
+__device__ __forceinline__ void clear_cells(uint2* cells, uint32_t n) {  // n even
+  uint4* c = reinterpret_cast<uint4*>(cells);
+  const uint32_t nt = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n / 2u; i += nt)
+    c[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+__device__ __forceinline__ void grid_done(const DSlots& G, uint32_t sub) {
+  if (G.cell == nullptr) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *G.cursor = 0u;
+  clear_cells(G.cell + (size_t)((sub & 1u) ^ 1u) * G.nbuckets, G.nbuckets);
+}
+
 // True when the interval [lo, hi] cannot reach [cmin, cmax] even allowing
 // for float rounding in the exact per-particle test (a relative margin of
 // 1e-5 is far above the few-ulp error of the subtractions and squares there).
@@ -1691,19 +1793,17 @@ constexpr uint32_t COLLIDE_THREADS = 256;      // 8 warps
 constexpr uint32_t COLLIDE_PER_WARP = 10;      // particles per warp, three lanes each
 constexpr uint32_t COLLIDE_CTAS = CHUNK / (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP);  // per chunk
 static_assert(COLLIDE_CTAS * (COLLIDE_THREADS / 32) * COLLIDE_PER_WARP == CHUNK, "chunk split");
-static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate(
-    const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
+template <class GRID>
+__global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate(
+    const DWorld* __restrict__ worlds, GRID G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
   pdl_trigger();
   // chunk and world records are fixed during a step: read before the wait
   const uint32_t cidx = blockIdx.x / COLLIDE_CTAS;
   const uint2 ch = chunks[cidx < nchunks ? cidx : 0u];
   const DWorld& W = worlds[ch.x];
-  pdl_wait();  // sorted entries from the scatter (and everything before it)
-  // this sub-step's scan is done with the cursor: clear it for the next one
-  // (whose scan runs after this kernel completes).  Engines without particle
-  // collisions have no grid (null cursor) but still run this kernel.
-  if (blockIdx.x == 0 && threadIdx.x == 0 && G.cursor != nullptr) *G.cursor = 0u;
+  pdl_wait();  // the grid's entries (and everything before them)
+  grid_done(G, sub);
   if (cidx >= nchunks || sub >= W.S) return;  // uniform over the CTA
   const uint32_t wl = threadIdx.x & 31u, grp = wl / 3u, row = wl - 3u * grp;
   const uint32_t i = ch.y + (blockIdx.x % COLLIDE_CTAS) * (COLLIDE_THREADS / 32 * COLLIDE_PER_WARP) +
@@ -1734,10 +1834,10 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate
       const uint32_t b0 = W.gb0 + (k == 0u ? (ho | 3u) : (hm | (k - 1u)));
       const uint32_t b1 = W.gb0 + (hm | k);
       const uint32_t b2 = W.gb0 + (k == 3u ? ho : (hm | (k + 1u)));
-      const uint2 r0 = G.range[b0], r1 = G.range[b1], r2 = G.range[b2];
-      visit_cell(G, p, cx - 1, cy, r0.x, r0.y, D, D2, c);
-      visit_cell(G, p, cx, cy, r1.x, r1.y, D, D2, c);
-      visit_cell(G, p, cx + 1, cy, r2.x, r2.y, D, D2, c);
+      const uint2 r0 = grid_head(G, sub, b0), r1 = grid_head(G, sub, b1), r2 = grid_head(G, sub, b2);
+      grid_visit(G, p, cx - 1, cy, b0, r0, D, D2, c);
+      grid_visit(G, p, cx, cy, b1, r1, D, D2, c);
+      grid_visit(G, p, cx + 1, cy, b2, r2, D, D2, c);
       contacts_finish(D, c);
     }
     long long sx = c.sx, sy = c.sy;
@@ -1798,17 +1898,17 @@ static __global__ void __launch_bounds__(COLLIDE_THREADS, 5) k_collide_integrate
 // against 0.24 ms).  Same contacts and the same fixed-point sums, so the
 // same bits.  One CTA per work chunk.
 constexpr uint32_t COLLIDE_P_THREADS = CHUNK;
-static __global__ void __launch_bounds__(COLLIDE_P_THREADS, 3) k_collide_particle(
-    const DWorld* __restrict__ worlds, DGrid G, const uint2* __restrict__ chunks,
+template <class GRID>
+__global__ void __launch_bounds__(COLLIDE_P_THREADS, 3) k_collide_particle(
+    const DWorld* __restrict__ worlds, GRID G, const uint2* __restrict__ chunks,
     uint32_t nchunks, uint32_t cur, uint32_t sub) {
   pdl_trigger();
   // chunk and world records are fixed during a step: read before the wait
   const uint32_t cidx = blockIdx.x;
   const uint2 ch = chunks[cidx < nchunks ? cidx : 0u];
   const DWorld& W = worlds[ch.x];
-  pdl_wait();  // sorted entries from the scatter (and everything before it)
-  // as in k_collide_integrate: the scan is done with the cursor
-  if (blockIdx.x == 0 && threadIdx.x == 0 && G.cursor != nullptr) *G.cursor = 0u;
+  pdl_wait();  // the grid's entries (and everything before them)
+  grid_done(G, sub);
   if (cidx >= nchunks || sub >= W.S) return;  // uniform over the CTA
   const uint32_t wl = threadIdx.x & 31u;
   const uint32_t i = ch.y + threadIdx.x;
@@ -1830,22 +1930,24 @@ static __global__ void __launch_bounds__(COLLIDE_P_THREADS, 3) k_collide_particl
       // buckets of cells cx - 1 .. cx + 1 in each row, as k_collide_integrate
       const int32_t st = cx >> 2;
       const uint32_t k = (uint32_t)cx & 3u;
+      uint32_t bk[9];
       uint2 r[9];
 #pragma unroll
       for (int row = 0; row < 3; ++row) {
         const int32_t cy = cy0 + row - 1;
         const uint32_t hm = (cell_hash(st, cy) << 2) & W.gmask;
         const uint32_t ho = (cell_hash(k == 0u ? st - 1 : st + 1, cy) << 2) & W.gmask;
-        r[3 * row] = G.range[W.gb0 + (k == 0u ? (ho | 3u) : (hm | (k - 1u)))];
-        r[3 * row + 1] = G.range[W.gb0 + (hm | k)];
-        r[3 * row + 2] = G.range[W.gb0 + (k == 3u ? ho : (hm | (k + 1u)))];
+        bk[3 * row] = W.gb0 + (k == 0u ? (ho | 3u) : (hm | (k - 1u)));
+        bk[3 * row + 1] = W.gb0 + (hm | k);
+        bk[3 * row + 2] = W.gb0 + (k == 3u ? ho : (hm | (k + 1u)));
       }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) r[j] = grid_head(G, sub, bk[j]);
 #pragma unroll
       for (int row = 0; row < 3; ++row)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
-          visit_cell(G, p, cx + j - 1, cy0 + row - 1, r[3 * row + j].x, r[3 * row + j].y, D, D2,
-                     c);
+          grid_visit(G, p, cx + j - 1, cy0 + row - 1, bk[3 * row + j], r[3 * row + j], D, D2, c);
       contacts_finish(D, c);
       if (c.hit) {
         p.x = fadd(p.x, unfix32(c.sx));
@@ -1887,10 +1989,16 @@ static __global__ void __launch_bounds__(COLLIDE_P_THREADS, 3) k_collide_particl
   W.prev[i] = q;
 }
 
-// positions of worlds whose step ended in buffer 1 go back to buffer 0
+// positions of worlds whose step ended in buffer 1 go back to buffer 0.
+// With an odd number of sub-steps the last collide pass (parity 0) cleared
+// parity 1's cell words of the slotted grid; parity 0's, which the first
+// sub-step of the next update uses, are cleared here (cells = null: nothing
+// to clear).
 static __global__ void __launch_bounds__(CHUNK) k_copy_back(const DWorld* __restrict__ worlds,
                                                      const uint2* __restrict__ chunks,
-                                                     uint32_t nchunks) {
+                                                     uint32_t nchunks, uint2* cells,
+                                                     uint32_t ncells) {
+  if (cells != nullptr) clear_cells(cells, ncells);
   if (blockIdx.x >= nchunks) return;
   const uint2 ch = chunks[blockIdx.x];
   const DWorld& W = worlds[ch.x];

@@ -194,12 +194,12 @@ extern "C" int b2d_collide_substeps_noalloc(float* d_pos_xy, float* d_prev_xy, s
     if ((e = launch(k_grid_scatter, nch, CHUNK, st, (const DWorld*)dW, G, (const uint2*)chunks,
                     nch, cur, s)) != cudaSuccess)
       return bad(e, "scatter launch");
-    if ((e = launch(k_collide_integrate, nch * COLLIDE_CTAS, COLLIDE_THREADS, st,
+    if ((e = launch(k_collide_integrate<DGrid>, nch * COLLIDE_CTAS, COLLIDE_THREADS, st,
                     (const DWorld*)dW, G, (const uint2*)chunks, nch, cur, s)) != cudaSuccess)
       return bad(e, "collide launch");
   }
-  if ((e = launch(k_copy_back, nch, CHUNK, st, (const DWorld*)dW, (const uint2*)chunks, nch)) !=
-      cudaSuccess)
+  if ((e = launch(k_copy_back, nch, CHUNK, st, (const DWorld*)dW, (const uint2*)chunks, nch,
+                  (uint2*)nullptr, 0u)) != cudaSuccess)
     return bad(e, "copy-back launch");
   return B2D_OK;
 }

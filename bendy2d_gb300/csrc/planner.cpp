@@ -44,6 +44,7 @@ bool PlanTuning::set(const std::string& k, double v) {
   else if (k == "bucket_factor") bucket_factor = (float)v;
   else if (k == "collide_thread_min") collide_thread_min = (uint32_t)v;
   else if (k == "large_max") large_max = (uint32_t)v;
+  else if (k == "grid_slot_max") grid_slot_max = (uint32_t)std::min(v, 4294967295.0);
   else return false;
   return true;
 }

@@ -110,7 +110,8 @@ int b2d_set_circle_static(b2d_solver* s, size_t index, int is_static);
 /* executor tunables (the autotuner sets these): serial_width, t_min, t_max,
  * pack_np, pack_nl, free_chunk, smem_max, warp_groups, max_groups,
  * width_per_thread, resident, res_max, stage_frac, bucket_factor,
- * collide_thread_min, large_max; they move
+ * collide_thread_min, large_max, grid_slot_max (collision particles up to
+ * which the grid is built by slot inserts, above by a counting sort); they move
  * work between executors and never change results; take effect at the next
  * update; B2D_ERR_ARG for an unknown key */
 int b2d_set_tuning(b2d_solver* s, const char* key, double value);
@@ -123,8 +124,9 @@ int b2d_update(b2d_solver* s, float dt);                    /* Solver::update, :
  * takes the timeout path of its first bulk-copy wait (device error word,
  * the copy in flight still lands, the group leaves), so b2d_synchronize
  * reports B2D_ERR_DEVICE.  B2D_FAULT_GRID_CAP (value > 0): the collision
- * grid hands out at most `value` sorted entries per sub-step; below the
- * particle count the scan refuses blocks instead of writing past them
+ * grid holds at most `value` overflow entries per sub-step (the entries of a
+ * bucket past its fixed slots; for the sorted grid, all entries); an
+ * insert past that is refused instead of written past the array
  * (B2D_ERR_DEVICE).  B2D_FAULT_ALLOC: the next `value` world-block
  * allocations fail as if cudaMallocAsync had (B2D_ERR_CUDA).  Value 0 turns
  * a fault off; the solver's state after a reported failure is unspecified

@@ -438,7 +438,8 @@ def test_config5_full_size_isolated_bodies_match_oracle(gpu):
     {"t_max": 64}, {"t_min": 256, "t_max": 256}, {"width_per_thread": 2.0},
     {"resident": 0}, {"serial_width": 1000.0}, {"serial_width": 0.0},
     {"max_groups": 1, "warp_groups": 1}, {"stage_frac": 0.0}, {"stage_frac": 2.0},
-    {"smem_max": 16384}, {"collide_thread_min": 0},
+    {"smem_max": 16384}, {"collide_thread_min": 0}, {"grid_slot_max": 0},
+    {"grid_slot_max": 0, "collide_thread_min": 0},
 ])
 def test_tunables_never_change_results(gpu, tuning):
     """Executor tunables move work between executors, group sizes, launch
