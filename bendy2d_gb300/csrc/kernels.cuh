@@ -715,15 +715,36 @@ __global__ void k_exec_serial(const DWorld* __restrict__ worlds, const uint2* __
   const float gx = W.gx, gy = W.gy, h = W.h;
   DWorld Wb;
   Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
+  // as in k_exec_serial_smem: link k + 1's positions are loaded before
+  // link k's stores and forwarded from link k's registers where it wrote
+  // them, so the global store-to-load round trip leaves the chain
+  const uint32_t nl1 = B.nl ? B.nl - 1u : 0u;
+  auto ends = [&](uint32_t k) {
+    const uint2 e = ab[k];  // body-local endpoints
+    return make_uint2(bidx[e.x], bidx[e.y]);
+  };
+  auto par = [&](uint32_t k) { return make_float2(rest[k], stiff[k]); };
   for (uint32_t s = 0; s < nsub; ++s) {
-    for (uint32_t it = 0; it < I; ++it) {
+    for (uint32_t it = 0; it < I && B.nl; ++it) {
+      uint2 e = ends(0), e1 = ends(nl1 < 1u ? nl1 : 1u);
+      float2 r = par(0), r1 = par(nl1 < 1u ? nl1 : 1u);
+      float2 pa = p[e.x], pb = p[e.y];
       for (uint32_t k = 0; k < B.nl; ++k) {
-        const uint2 e = ab[k];  // body-local endpoints
-        const uint32_t ia = bidx[e.x], ib = bidx[e.y];
-        float2 pa = p[ia], pb = p[ib];
-        link_solve_plain(pa, pb, rest[k], stiff[k]);
-        p[ia] = pa;
-        p[ib] = pb;
+        const uint32_t k2 = k + 2u < nl1 ? k + 2u : nl1;
+        const uint2 e2 = ends(k2);
+        const float2 r2 = par(k2);
+        float2 na = p[e1.x], nb = p[e1.y];  // link k + 1's, before link k's stores
+        link_solve_plain(pa, pb, r.x, r.y);
+        p[e.x] = pa;
+        p[e.y] = pb;
+        na = e1.x == e.x ? pa : (e1.x == e.y ? pb : na);
+        nb = e1.y == e.x ? pa : (e1.y == e.y ? pb : nb);
+        pa = na;
+        pb = nb;
+        e = e1;
+        e1 = e2;
+        r = r1;
+        r1 = r2;
       }
     }
     if (FULL) {
@@ -818,27 +839,40 @@ __global__ void k_exec_serial_smem(const DWorld* __restrict__ worlds,
       const float gx = W.gx, gy = W.gy, h = W.h;
       DWorld Wb;
       Wb.bx = W.bx; Wb.by = W.by; Wb.bw = W.bw; Wb.bh = W.bh;
-      // link k's endpoints and parameters, loaded one link ahead (they do not
-      // depend on the positions, so their latency leaves the chain)
+      // Link k's endpoints and parameters are loaded two links ahead and its
+      // positions one link ahead, before link k - 1's stores: a position
+      // that link k - 1 writes is taken from its registers instead
+      // (forwarded), so neither the parameter loads nor the shared-memory
+      // store-to-load round trip sit on the chain, which is then one link
+      // solve and two selects per link.
       auto link_at = [&](uint32_t k, uint2& e, float2& r) {
         e = STAGED ? ab[k] : __ldg(ab + k);
         r = STAGED ? rs[k] : make_float2(__ldg(grest + k), __ldg(gstiff + k));
       };
+      const uint32_t nl1 = B.nl ? B.nl - 1u : 0u;
       for (uint32_t s = 0; s < nsub; ++s) {
         for (uint32_t it = 0; it < I && B.nl; ++it) {
-          uint2 e;
-          float2 r;
+          uint2 e, e1;
+          float2 r, r1;
           link_at(0, e, r);
+          link_at(nl1 < 1u ? nl1 : 1u, e1, r1);
+          float2 pa = p[e.x], pb = p[e.y];
           for (uint32_t k = 0; k < B.nl; ++k) {
-            uint2 en;
-            float2 rn;
-            link_at(k + 1 < B.nl ? k + 1 : k, en, rn);
-            float2 pa = p[e.x], pb = p[e.y];
+            uint2 e2;
+            float2 r2;
+            link_at(k + 2u < nl1 ? k + 2u : nl1, e2, r2);
+            float2 na = p[e1.x], nb = p[e1.y];  // link k + 1's, before link k's stores
             link_solve_plain(pa, pb, r.x, r.y);
             p[e.x] = pa;
             p[e.y] = pb;
-            e = en;
-            r = rn;
+            na = e1.x == e.x ? pa : (e1.x == e.y ? pb : na);
+            nb = e1.y == e.x ? pa : (e1.y == e.y ? pb : nb);
+            pa = na;
+            pb = nb;
+            e = e1;
+            r = r1;
+            e1 = e2;
+            r1 = r2;
           }
         }
         if (FULL) {
