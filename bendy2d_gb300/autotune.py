@@ -44,7 +44,7 @@ DEFAULTS = {
     "max_groups": 15,
     "serial_width": 2.0,
     "resident": 1,
-    "stage_frac": 0.67,
+    "stage_frac": 1.01,
     "bucket_factor": 2.0,
     "collide_thread_min": 131072,
     "grid_slot_max": 262144,

@@ -40,7 +40,10 @@ struct PlanTuning {
   float width_per_thread = 0.5f;    // T = pow2 >= avg width / this (issue-bound: wide groups win)
   uint32_t resident = 1;            // load a body's whole schedule when it fits
   uint32_t res_max = 227 * 1024;    // shared bytes per group for body + resident schedule
-  float stage_frac = 0.67f;         // serial bodies with chains >= this x the longest: solo packs
+  float stage_frac = 1.01f;         // serial bodies with chains >= this x the longest: solo
+                                    // packs, links staged in shared memory (default: none;
+                                    // with positions forwarded in registers ordinary packs
+                                    // run the longest chains faster)
   float bucket_factor = 2.0f;       // collision-grid buckets per world: pow2 >= this x particles
   uint32_t collide_thread_min = 131072;  // particles in the collide pass from which it runs
                                          // one thread per particle (else three lanes each)
