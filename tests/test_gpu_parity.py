@@ -546,3 +546,49 @@ def test_programmatic_launches_do_not_change_results(gpu):
         a.update(sc.dt)
         b.update(sc.dt)
     assert_same_state(solver_state(a), solver_state(b), "programmatic vs serial launches")
+
+
+def _clumped_cloths(seed, sub_steps, n_bodies=4):
+    """Cloth grids plus a 3 x 3 grid packed into one collision cell (nine
+    entries in one bucket: five in its overflow chain), particle collisions."""
+    from bendy2d_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    bodies = [scenes.grid_body(16, 16, rng.uniform(0.0, 80.0, 2), 1.0, 0.01, rng)
+              for _ in range(n_bodies)]
+    bodies.append(scenes.grid_body(3, 3, (95.3, 95.3), 0.05, 0.0, rng))
+    sc = scenes._assemble(f"clumped_s{sub_steps}", bodies, bounds=(0.0, 0.0, 100.0, 100.0),
+                          sub_steps=sub_steps, link_iters=2, collide=1)
+    sc.prev = scenes._velocity_prev(sc.pos, rng, 0.5, sc.dt / sc.sub_steps)
+    return sc
+
+
+@pytest.mark.parametrize("slot_max", [1 << 30, 0])
+def test_collision_grid_odd_and_mixed_sub_steps(gpu, slot_max):
+    """The slotted grid double-buffers its cell words by sub-step parity and
+    clears parity 0 in the copy-back when an update has an odd number of
+    sub-steps; overflow chains hold a bucket's entries past its slots.
+    Several updates of worlds with 1, 3 and 4 sub-steps, alone and in one
+    batch (odd and even sub-step counts together), with a dense clump, in
+    both grid forms (slot_max 0: the sorted grid): every world matches the
+    oracle."""
+    from bendy2d_gb300 import Batch
+    from oracle import load_scene
+    worlds = [_clumped_cloths(61, 3), _clumped_cloths(62, 4), _clumped_cloths(63, 1)]
+    alone = [w.to_solver() for w in worlds]
+    for s in alone:
+        s.set_tuning(grid_slot_max=slot_max)
+    together = [w.to_solver() for w in worlds]
+    b = Batch(together)
+    b.set_tuning(grid_slot_max=slot_max)
+    oracles = [load_scene(w) for w in worlds]
+    for step in range(4):
+        for s, w, o in zip(alone, worlds, oracles):
+            s.update(w.dt)
+            assert o.update(w.dt) == 0
+        b.update(worlds[0].dt)
+        for s, t, o, w in zip(alone, together, oracles, worlds):
+            assert_same_state(solver_state(s), oracle_state(o), f"{w.name} alone, update {step}")
+            assert_same_state(solver_state(t), oracle_state(o), f"{w.name} batched, update {step}")
+    b.close()
+    for s in alone:
+        s.close()
