@@ -118,7 +118,14 @@ Engine::~Engine() {
   for (auto& e : evpool_) cudaEventDestroy(e);
   for (auto& a : aux_) cudaStreamDestroy(a);
   for (auto& a : lx_) cudaStreamDestroy(a);
+  if (ist_) cudaStreamDestroy(ist_);
   if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine::install_beside(bool on) {
+  if (on && !ist_) B2D_CUDA(cudaStreamCreateWithFlags(&ist_, cudaStreamNonBlocking));
+  beside_ = on;
+  return OK;
 }
 
 void Engine::invalidate_graph() {
@@ -207,7 +214,7 @@ int Engine::fill_world_record(uint32_t slot) {
   int st = ensure_table(slots_.size());
   if (st != OK) return st;
   B2D_CUDA(cudaMemcpyAsync(d_worlds_ + slot, &h_worlds_[slot], sizeof(DWorld),
-                           cudaMemcpyHostToDevice, stream_));
+                           cudaMemcpyHostToDevice, up_stream()));
   return OK;
 }
 
@@ -251,14 +258,15 @@ int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
     last_error = "cudaMallocAsync: injected allocation failure";
     return ERR_CUDA;
   }
-  B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&block), L.total, stream_));
+  const cudaStream_t up = up_stream();
+  B2D_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&block), L.total, up));
   std::vector<unsigned char> stage(L.total);
   write_block(img, L, stage.data());
-  cudaError_t ce = cudaMemcpyAsync(block, stage.data(), L.total, cudaMemcpyHostToDevice, stream_);
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);  // the staging buffer is pageable
+  cudaError_t ce = cudaMemcpyAsync(block, stage.data(), L.total, cudaMemcpyHostToDevice, up);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(up);  // the staging buffer is pageable
   if (ce != cudaSuccess) {
     last_error = std::string("uploading a world block: ") + cudaGetErrorString(ce);
-    cudaFreeAsync(block, stream_);
+    cudaFreeAsync(block, up);
     return ERR_CUDA;
   }
   uint32_t slot;
@@ -277,7 +285,13 @@ int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
   s.live = true;
   dev_bytes_ += L.total;
   lists_dirty_ = true;
-  const int st = fill_world_record(slot);
+  int st = fill_world_record(slot);
+  // beside a step in flight: the record must have landed before the next
+  // step, which the caller launches on the main stream
+  if (st == OK && beside_ && cudaStreamSynchronize(ist_) != cudaSuccess) {
+    last_error = "uploading a world record";
+    st = ERR_CUDA;
+  }
   if (st != OK) {
     remove(slot);
     return st;
@@ -304,8 +318,8 @@ int Engine::set_dt(uint32_t slot, float dt) {
   s.dt = dt;
   h_worlds_[slot].h = dt * (1.0f / (float)h_worlds_[slot].S);  // src/solver.rs:107-108
   B2D_CUDA(cudaMemcpyAsync(&d_worlds_[slot].h, &h_worlds_[slot].h, sizeof(float),
-                           cudaMemcpyHostToDevice, stream_));
-  B2D_CUDA(cudaStreamSynchronize(stream_));
+                           cudaMemcpyHostToDevice, up_stream()));
+  B2D_CUDA(cudaStreamSynchronize(up_stream()));
   return OK;
 }
 
@@ -580,6 +594,10 @@ int Engine::rebuild_lists() {
       for (const GroupBody& gb : s.img.groups)
         if (gb.res) ++res_count[std::make_tuple(gb.T, !s.img.ext, log2c(gb.region + gb.res))];
   wlaunch_.assign(slots_.size(), WorldLaunch());
+  // world records whose grid ranges moved (a world joined or left before
+  // them) go up in one copy after the loop: one pageable copy per record
+  // waited for the stream each time (~2 ms per step for 640 worlds)
+  uint32_t rec_lo = UINT32_MAX, rec_hi = 0;
   for (uint32_t si = 0; si < slots_.size(); ++si) {
     const Slot& s = slots_[si];
     if (!s.live) continue;
@@ -674,8 +692,8 @@ int Engine::rebuild_lists() {
           h_worlds_[si].gb0 = (uint32_t)nbuckets;
           h_worlds_[si].gmask = nbw - 1;
           h_worlds_[si].gp0 = (uint32_t)np_pp;
-          B2D_CUDA(cudaMemcpyAsync(d_worlds_ + si, &h_worlds_[si], sizeof(DWorld),
-                                   cudaMemcpyHostToDevice, stream_));
+          rec_lo = std::min(rec_lo, si);
+          rec_hi = std::max(rec_hi, si);
         }
         nbuckets += nbw;
         np_pp += im.params.np;
@@ -684,6 +702,12 @@ int Engine::rebuild_lists() {
       np_ext += im.params.np;
     }
   }
+  // h_worlds_ mirrors the device table, so the records between two moved
+  // ones can go up with them
+  if (rec_lo <= rec_hi)
+    B2D_CUDA(cudaMemcpyAsync(d_worlds_ + rec_lo, &h_worlds_[rec_lo],
+                             (size_t)(rec_hi - rec_lo + 1) * sizeof(DWorld),
+                             cudaMemcpyHostToDevice, stream_));
   // size each class to its largest member; a resident class whose largest
   // body and largest schedule do not fit together streams instead
   for (LaunchClass& c : classes_) {

@@ -147,6 +147,12 @@ class Engine {
   // and registers the world; the image is consumed
   int plan(const WorldHost& w, WorldImage* img, std::string* why);
   int add_planned(WorldHost* w, WorldImage&& img, uint32_t* slot);
+  // While on, add_planned() and set_dt() upload on a stream of their own
+  // and wait for that stream only, so that they can run while a step
+  // launched on the main stream is in flight (the server installs the next
+  // tick's worlds that way); the step in flight reads neither the new
+  // world's block nor its record.
+  int install_beside(bool on);
   int remove(uint32_t slot);
   int set_dt(uint32_t slot, float dt);
   int set_params(uint32_t slot);          // gravity / bounds changed on the host mirror
@@ -194,6 +200,9 @@ class Engine {
 
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
+  cudaStream_t ist_ = nullptr;  // install_beside's stream
+  bool beside_ = false;
+  cudaStream_t up_stream() const { return beside_ ? ist_ : stream_; }
   cudaStream_t aux_[2] = {nullptr, nullptr};  // graph branches (circles/polygons)
   static constexpr uint32_t kLinkBranches = 7;
   cudaStream_t lx_[kLinkBranches] = {};       // graph branches of the link phase

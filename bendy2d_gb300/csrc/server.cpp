@@ -3,16 +3,18 @@
 // A request is a world (a copy of a solver's contents) plus a number of
 // Solver::update calls.  A worker thread repeats one tick:
 //   1. take queued requests, first come first served, while the device bytes
-//      of the resident worlds plus the candidate stay within the budget, and
-//      install (upload) the ones planned during the previous tick;
+//      of the resident worlds plus the candidate stay within the budget;
 //   2. launch one Solver::update for every resident world, all in one launch
 //      sequence of a shared Engine (the same batched kernels as
-//      b2d_batch_update), and plan the requests taken in step 1 on the host
-//      while it runs;
+//      b2d_batch_update), and while it runs plan the requests taken in
+//      step 1 on the host and install them (their uploads go to the engine's
+//      install stream, so the device keeps stepping);
 //   3. wait, then retire requests that reached their step count: copy the
 //      state back, free the world's device block, record the latency.
-// Requests that arrive while a tick runs wait in the queue and join within
-// two ticks, so work overlaps on the device as memory frees up.  World state
+// Requests that arrive while a tick runs wait in the queue and join the
+// tick after next at the latest, so work overlaps on the device as memory
+// frees up.  On an idle device a request is planned and installed at once.
+// World state
 // stays device-resident across ticks.  Every world is computed independently
 // (per-world grids, order-independent sums), so a result is bit-identical
 // whether the request ran alone or in a mix.
@@ -223,6 +225,35 @@ void Server::loop() {
     if (st != OK) fail(r, why.empty() ? eng->last_error : why);
     else planned.emplace_back(r, std::move(img));
   };
+  // install the planned requests: they join the next tick
+  auto install = [&]() {
+    for (auto& pr : planned) {
+      Req* r = pr.first;
+      bool cancelled;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        cancelled = r->cancel;
+      }
+      if (cancelled) {
+        drop(r, SERVE_CANCELLED, "request cancelled");
+        continue;
+      }
+      uint32_t slot = 0;
+      int st = eng->add_planned(&r->world, std::move(pr.second), &slot);
+      if (st == OK) st = eng->set_dt(slot, r->dt);
+      if (st != OK) {
+        fail(r, eng->last_error);
+        continue;
+      }
+      std::lock_guard<std::mutex> lk(mu_);
+      r->slot = slot;
+      r->t_admit = Clock::now();
+      r->state = SERVE_RUNNING;
+      active_.push_back(r);
+      ++stats_.admitted;
+    }
+    planned.clear();
+  };
   for (;;) {
     std::vector<Req*> taken;
     std::vector<std::pair<int, uint64_t>> faults;
@@ -254,36 +285,11 @@ void Server::loop() {
       std::lock_guard<std::mutex> lk(mu_);
       idle = active_.empty();
     }
-    if (idle) {
+    if (idle) {  // nothing on the device: plan and install now
       for (Req* r : taken) plan(r);
       taken.clear();
+      install();
     }
-    for (auto& pr : planned) {
-      Req* r = pr.first;
-      bool cancelled;
-      {
-        std::lock_guard<std::mutex> lk(mu_);
-        cancelled = r->cancel;
-      }
-      if (cancelled) {
-        drop(r, SERVE_CANCELLED, "request cancelled");
-        continue;
-      }
-      uint32_t slot = 0;
-      int st = eng->add_planned(&r->world, std::move(pr.second), &slot);
-      if (st == OK) st = eng->set_dt(slot, r->dt);
-      if (st != OK) {
-        fail(r, eng->last_error);
-        continue;
-      }
-      std::lock_guard<std::mutex> lk(mu_);
-      r->slot = slot;
-      r->t_admit = Clock::now();
-      r->state = SERVE_RUNNING;
-      active_.push_back(r);
-      ++stats_.admitted;
-    }
-    planned.clear();
     std::vector<Req*> act;
     const Clock::time_point ts = Clock::now();
     {
@@ -300,9 +306,15 @@ void Server::loop() {
     bool any_steps = false;
     for (Req* r : act) any_steps |= r->done < r->steps;
     if (any_steps) st = eng->step();
-    // the requests taken this tick are planned on the host while it runs
+    // the requests taken this tick are planned and installed while it
+    // runs (their uploads on the engine's install stream)
     const Clock::time_point tp = Clock::now();
     for (Req* r : taken) plan(r);
+    if (any_steps && st == OK) {
+      eng->install_beside(true);
+      install();
+      eng->install_beside(false);
+    }
     const Clock::time_point tq = Clock::now();
     if (any_steps && st == OK) st = eng->sync();
     const Clock::time_point tr = Clock::now();
