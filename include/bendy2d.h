@@ -241,9 +241,9 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
  * first come first served while the device bytes of resident worlds stay
  * within the budget, steps every resident world once per tick in one launch
  * sequence, and retires finished requests.  A request taken from the queue
- * is planned on the host while the current tick runs and joins the next
- * one (it stays B2D_SERVE_QUEUED until then).  Results are bit-identical to
- * running the request alone. */
+ * is planned on the host and installed on the device while the current
+ * tick runs, and joins the next one (it stays B2D_SERVE_QUEUED until it is
+ * installed).  Results are bit-identical to running the request alone. */
 #define B2D_SERVE_QUEUED 0
 #define B2D_SERVE_RUNNING 1
 #define B2D_SERVE_DONE 2
@@ -252,9 +252,9 @@ int b2d_batch_set_tuning(b2d_batch* b, const char* key, double value);
 typedef struct {
   uint64_t submitted, admitted, completed, failed, queued, active;
   uint64_t ticks, particle_substeps, resident_bytes;
-  /* worker wall time, nanoseconds: admitting (planning, also while a tick
-   * runs, + upload), stepping (launch + wait, minus that planning), retiring
-   * (download + release) */
+  /* worker wall time, nanoseconds: admitting (planning and installing,
+   * mostly while a tick runs), stepping (launch + wait, minus the admitting
+   * done meanwhile), retiring (download + release) */
   uint64_t admit_ns, step_ns, retire_ns;
   uint64_t cancelled, resident_particles;
 } b2d_server_stats;
