@@ -1035,7 +1035,10 @@ int Engine::launch_all(bool profiling) {
       });
     }
     end_pass();
-    if (any_pp_ && grid_slotted_) {
+    // (worlds with collision flags but no solver particles, such as only
+    // circles, take part in the sub-step loop without work chunks: the
+    // particle kernels below are skipped when there are none)
+    if (any_pp_ && grid_slotted_ && nch) {
       // the cell words of this parity are all zero here (cleared by the
       // previous sub-step's collide pass, or by k_copy_back); worlds whose
       // link executor inserted their particles skip the insert pass
@@ -1044,7 +1047,7 @@ int Engine::launch_all(bool profiling) {
           lk(launch_k(k_grid_insert, dim3(nch), dim3(CHUNK), 0, stream_, !profiling, W, GS, CH,
                       nch, cur, s));
         });
-    } else if (any_pp_) {
+    } else if (any_pp_ && nch) {
       // counts are all zero here: the scan of the previous sub-step cleared them.
       // Small grids: one 256-thread CTA per 1,024-bucket tile; large ones:
       // 16,384-bucket tiles over at most one 1024-thread CTA per SM.
@@ -1072,7 +1075,7 @@ int Engine::launch_all(bool profiling) {
       });
     }
     if (nre) edge(ax, stream_);
-    timed("collide_integrate", [&] {
+    if (nch) timed("collide_integrate", [&] {
       if (grid_slotted_ || !any_pp_) {
         if (collide_per_particle_)
           lk(launch_k(k_collide_particle<DSlots>, dim3(nch), dim3(COLLIDE_P_THREADS), 0, stream_,
@@ -1098,7 +1101,7 @@ int Engine::launch_all(bool profiling) {
     });
     // an odd sub-step count leaves parity 0's cell words for k_copy_back to clear
     const bool clear0 = any_pp_ && grid_slotted_ && (smax_ext_ & 1u);
-    timed("copy_back", [&] {
+    if (nch) timed("copy_back", [&] {
       k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch, clear0 ? GS.cell : nullptr,
                                                clear0 ? GS.nbuckets : 0u);
     });

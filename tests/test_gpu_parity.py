@@ -264,6 +264,22 @@ def test_circle_links_and_static_circles(gpu):
     check(sc, 10, "circle links")
 
 
+@pytest.mark.parametrize("collide", [2, 7])
+def test_collision_flags_without_solver_particles(gpu, collide):
+    """A world with collision flags but only circles and a polygon (no
+    solver particles) runs the sub-step pipeline with no particle work:
+    no particle kernel is launched, the circles and the polygon move as in
+    the oracle."""
+    from bendy2d_gb300 import scenes
+    rng = np.random.default_rng(8)
+    circles = [scenes._circle(rng.uniform(20, 80, 2), rng.uniform(1, 4), False) for _ in range(6)]
+    polys = [{"points": scenes.convex_polygon(rng, (50.0, 50.0), 10.0, 5), "static": False}]
+    sc = scenes._assemble("no_particles", [], circles=circles, polygons=polys,
+                          bounds=(0.0, 0.0, 100.0, 100.0), sub_steps=3, link_iters=1,
+                          collide=collide)
+    check(sc, 5, f"collision flags {collide}, no solver particles")
+
+
 def test_empty_and_degenerate_worlds(gpu):
     from bendy2d_gb300 import Solver
     s = Solver()
