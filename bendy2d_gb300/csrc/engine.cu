@@ -303,7 +303,12 @@ int Engine::add_planned(WorldHost* w, WorldImage&& img, uint32_t* out_slot) {
 int Engine::remove(uint32_t slot) {
   if (slot >= slots_.size() || !slots_[slot].live) return ERR_INDEX;
   Slot& s = slots_[slot];
-  B2D_CUDA(cudaFreeAsync(s.block, stream_));
+  // An engine that installs beside its steps frees on the install stream,
+  // so that a later install reusing the block has no cross-stream wait on
+  // a step in flight (the pool would otherwise order the reuse after the
+  // main stream); its callers remove a world only once no launched step
+  // uses it (the server: after the tick's synchronisation).
+  B2D_CUDA(cudaFreeAsync(s.block, ist_ ? ist_ : stream_));
   dev_bytes_ -= s.L.total;
   s = Slot();
   free_slots_.push_back(slot);
