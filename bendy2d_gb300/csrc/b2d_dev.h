@@ -141,9 +141,10 @@ enum : uint32_t { ERR_BIT_TMA_TIMEOUT = 1u, ERR_BIT_GRID_OVERFLOW = 2u };
 // for the copy in flight to land, leave) without a real timeout.
 enum : uint32_t { FAULT_BIT_WAIT = 1u };
 
-// Extension broadphase: hashed uniform grid built by a counting sort each
-// sub-step.  Every world with particle collisions owns a power-of-two range
-// of buckets; a bucket's entries are contiguous in `sorted`.
+// Extension broadphase: hashed uniform grid, sorted form (large grids and
+// the allocation-free entry point): built by a counting sort each sub-step.
+// Every world with particle collisions owns a power-of-two range of
+// buckets; a bucket's entries are contiguous in `sorted`.
 // bucket scan tiles: 1,024 buckets (256 threads x 4 each) for grids of up to
 // SCAN_SMALL_MAX buckets, else 16,384 (four sub-tiles of 1024 threads x 4)
 constexpr uint32_t SCAN_SMALL_TILE = 1024;

@@ -1416,12 +1416,13 @@ __global__ void __launch_bounds__(THREADS) k_rigid(const DWorld* __restrict__ wo
 // ----------------------------------------------------------------------------
 // Extension: particle collisions (not in the reference, whose solver
 // particles only interact through links, src/solver.rs:143-188).  Hashed
-// uniform grid (counting sort per sub-step); Jacobi contacts against every
-// particle of the 9 surrounding cells, summed in fixed point so that the
-// result does not depend on the visiting order.
+// uniform grid, rebuilt every sub-step (slot inserts, or a counting sort for
+// large grids); Jacobi contacts against every particle of the 9 surrounding
+// cells, summed in fixed point so that the result does not depend on the
+// visiting order.
 // ----------------------------------------------------------------------------
-// particles per work chunk: one CTA of the count / scatter / copy-back
-// kernels, four collide CTAs of 8 warps x 10 particles
+// particles per work chunk: one CTA of the insert / count / scatter /
+// copy-back kernels, four collide CTAs of 8 warps x 10 particles
 constexpr uint32_t CHUNK = 320;
 
 // Bucket entry: {pos.x bits, pos.y bits, cell x, cell y}.  Cells that hash
