@@ -206,3 +206,24 @@ def test_unknown_tunable_is_rejected(native_lib):
     with pytest.raises(B2DError) as e:
         s.set_tuning(no_such_knob=1.0)
     assert "unknown tunable" in str(e.value)
+
+
+
+TUNABLES = ["serial_width", "t_min", "t_max", "pack_np", "pack_nl", "free_chunk", "smem_max",
+            "warp_groups", "max_groups", "width_per_thread", "resident", "res_max",
+            "stage_frac", "bucket_factor", "collide_thread_min", "large_max", "grid_slot_max"]
+
+
+def test_every_documented_tunable_is_accepted(native_lib):
+    """Each tunable is listed in the header's b2d_set_tuning comment and
+    accepted by the library; the autotuner searches only known ones."""
+    from pathlib import Path
+    from bendy2d_gb300 import Solver
+    from bendy2d_gb300.autotune import DEFAULTS
+    hdr = (Path(__file__).resolve().parents[1] / "include" / "bendy2d.h").read_text()
+    block = hdr[hdr.index("/* executor tunables"):hdr.index("int b2d_set_tuning")]
+    s = Solver()
+    for k in TUNABLES:
+        assert k in block, k
+        s.set_tuning(**{k: DEFAULTS.get(k, 1.0)})
+    assert set(DEFAULTS) <= set(TUNABLES)
