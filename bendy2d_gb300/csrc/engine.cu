@@ -573,6 +573,7 @@ int Engine::rebuild_lists() {
   rigid_ext_.clear();
   rigid_wide_full_ = rigid_wide_ext_ = false;
   smax_ext_ = 0;
+  any_odd_ext_ = false;
   any_pp_ = false;
   any_count_ = false;
   size_t np_ext = 0;
@@ -686,6 +687,7 @@ int Engine::rebuild_lists() {
         rigid_wide_ext_ |= wide;
       }
       smax_ext_ = std::max(smax_ext_, im.params.S);
+      any_odd_ext_ |= (im.params.S & 1u) != 0u;
       if (im.params.flags & COLLIDE_PP) {
         any_pp_ = true;
         // this world's bucket range: a power of two >= 2 x its particles
@@ -1106,7 +1108,8 @@ int Engine::launch_all(bool profiling) {
     });
     // an odd sub-step count leaves parity 0's cell words for k_copy_back to clear
     const bool clear0 = any_pp_ && grid_slotted_ && (smax_ext_ & 1u);
-    if (nch) timed("copy_back", [&] {
+    // nothing to copy back or clear when every world has an even count
+    if (nch && (any_odd_ext_ || clear0)) timed("copy_back", [&] {
       k_copy_back<<<nch, CHUNK, 0, stream_>>>(W, CH, nch, clear0 ? GS.cell : nullptr,
                                                clear0 ? GS.nbuckets : 0u);
     });

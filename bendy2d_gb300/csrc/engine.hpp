@@ -236,6 +236,7 @@ class Engine {
   size_t wlists_cap_ = 0;
   size_t off_rigid_ext_ = 0;
   uint32_t smax_ext_ = 0;
+  bool any_odd_ext_ = false;  // a collision world ends its update in the second position buffer
   bool plain_ = false;
   struct WorldLaunch {  // this world's ranges in the lists (plain mode)
     std::vector<std::pair<uint32_t, uint32_t>> cls;  // per class: (offset, count)
