@@ -633,6 +633,8 @@ def run_profile_config(args, torch) -> None:
     else:
         sc = scenes.config5(seed=0, mode=MODE_FAST)
         runner, dt, units = sc.to_solver(), sc.dt, sc.n_particles * sc.sub_steps
+    if args.tuning:
+        runner.set_tuning(**json.loads(args.tuning))
     for _ in range(args.warmup):
         runner.update(dt)
     runner.synchronize()
@@ -692,6 +694,9 @@ def main():
     ap.add_argument("--profile-config", type=int, choices=[1, 2, 3, 5], default=0,
                     help="run only --warmup + --steps updates of one configuration (the "
                          "command the ncu summaries profile) and print its step time")
+    ap.add_argument("--tuning", default="", metavar="JSON",
+                    help="with --profile-config / --profile-large: executor tunables to set "
+                         "first, as a JSON object (grid_slot_max 0: the sorted collision grid)")
     ap.add_argument("--profile-large", type=int, default=0, metavar="SIDE",
                     help="like --profile-config, for one SIDE x SIDE cloth without "
                          "collisions (8 sub-steps, 4 link passes): a body for the "
