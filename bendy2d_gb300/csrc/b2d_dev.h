@@ -30,6 +30,12 @@ constexpr uint32_t GRID_IN_LINKS = 8u;
 // integrate ops carry the body-local particle index with this bit set.
 constexpr uint32_t OP_INTEG = 0x80000000u;
 constexpr uint32_t OP_WIDE = 0xFFFFFFFFu;
+// Whole-update schedules only: a padding entry {0, OP_NOP} that does
+// nothing.  Within a level the link solves come first, padded to a whole
+// number of warps, then the bounds+integrate ops, so that no warp runs both
+// code paths (the ops of a level are independent, so their order within the
+// level cannot change any result).
+constexpr uint32_t OP_NOP = 0xFFFFFFFEu;
 
 // A body is a set of solver particles run by one executor unit: a union of
 // whole link-connected components, so no link crosses two bodies.
@@ -60,6 +66,7 @@ struct DPoly {
 //                                             of up to 65535 particles)
 //                {link index, OP_WIDE}       (larger bodies)
 //     integrate  {particle, OP_INTEG}
+//     padding    {0, OP_NOP}                 (whole-update schedules)
 // A segment is a whole level or a piece of one; a group barrier follows
 // every segment.
 constexpr uint32_t SCHED_CHUNK_WORDS = 4096;

@@ -390,6 +390,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
 
   // One op: a link solve or (FULL) bounds + integrate of one particle.
   auto run = [&](uint2 op) {
+    if (FULL && op.y == OP_NOP) return;  // padding of a whole-update schedule
     if (FULL && op.y == OP_INTEG) {
       float2 p, q;
       if (SMEM) {
@@ -643,6 +644,7 @@ __global__ void __launch_bounds__(1024) k_exec_large(const DWorld* __restrict__ 
     if (CLUSTER) stc_f32x2(dsmem_addr(a, j >> log2per), v); else sts_f32x2(a, v);
   };
   auto run = [&](uint2 op) {
+    if (FULL && op.y == OP_NOP) return;  // padding of a whole-update schedule
     if (FULL && op.y == OP_INTEG) {  // bounds + integrate, src/solver.rs:155-158, :118-121
       float2 p = ld(sp_a, op.x), q = ld(sq_a, op.x);
       solve_bounds(p, q, Wb);

@@ -96,8 +96,41 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
     std::vector<uint32_t> fill(start.begin(), start.end());
     for (size_t i = 0; i < total; ++i) sorted[fill[lvl_of[i]]++] = op_of[i];
   }
-  for (size_t i = 0; i < total; ++i) {  // self-check: ops name the body's links/particles
-    const uint32_t op = sorted[i];
+  // Whole-update schedules: within each level the link solves first, then
+  // the bounds+integrate ops, the links padded with OP_NOP entries to a
+  // whole number of warps (a level's ops are independent, so this order
+  // gives the same results).  A warp then runs one kind only.  Padding
+  // stays within the power of two above the widest level, so a group that
+  // ran every level with one op per thread still does.
+  constexpr uint32_t NOP_ID = 0xFFFFFFFFu;
+  if (full) {
+    uint32_t maxw0 = 0;
+    for (uint32_t l = 1; l <= maxl; ++l) maxw0 = std::max(maxw0, start[l + 1] - start[l]);
+    uint32_t cap = 1;
+    while (cap < maxw0) cap <<= 1;
+    std::vector<uint32_t> out, nstart(maxl + 2, 0);
+    out.reserve(total + 32 * (size_t)maxl);
+    for (uint32_t l = 1; l <= maxl; ++l) {
+      nstart[l] = (uint32_t)out.size();
+      const uint32_t b = start[l], e = start[l + 1];
+      uint32_t nlink = 0;
+      for (uint32_t i = b; i < e; ++i)
+        if (!(sorted[i] & OP_INTEG)) {
+          out.push_back(sorted[i]);
+          ++nlink;
+        }
+      const uint32_t ninteg = (e - b) - nlink;
+      const uint32_t pad = (32u - nlink % 32u) % 32u;
+      if (nlink && ninteg && pad && nlink + pad + ninteg <= cap) out.insert(out.end(), pad, NOP_ID);
+      for (uint32_t i = b; i < e; ++i)
+        if (sorted[i] & OP_INTEG) out.push_back(sorted[i]);
+    }
+    nstart[maxl + 1] = (uint32_t)out.size();
+    sorted.swap(out);
+    start.swap(nstart);
+  }
+  for (uint32_t op : sorted) {  // self-check: ops name the body's links/particles
+    if (op == NOP_ID) continue;
     if ((op & OP_INTEG) ? (op & ~OP_INTEG) >= np : op >= nl) std::abort();
   }
   // cut the level sequence into chunks (a level may span chunks)
@@ -116,7 +149,10 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
     stream.insert(stream.end(), seg_end.begin(), seg_end.end());
     if ((stream.size() - at) % 2) stream.push_back(0);
     for (uint32_t op : chunk_ops) {
-      if (op & OP_INTEG) {
+      if (op == NOP_ID) {
+        stream.push_back(0);
+        stream.push_back(OP_NOP);
+      } else if (op & OP_INTEG) {
         stream.push_back(op & ~OP_INTEG);
         stream.push_back(OP_INTEG);
       } else if (narrow) {
