@@ -79,6 +79,7 @@ struct DSched {
   uint32_t off, words;       // the chunks are contiguous: stream[off, off + words)
   uint32_t len0;             // words of the first chunk
   uint32_t maxw;             // most ops in one segment
+  uint32_t nop_pad;          // 1: the schedule holds OP_NOP padding entries
 };
 
 // 1 / c when c is a positive normal power of two (then x / c == x * (1/c)

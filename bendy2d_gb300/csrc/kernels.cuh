@@ -389,8 +389,12 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   }
 
   // One op: a link solve or (FULL) bounds + integrate of one particle.
-  auto run = [&](uint2 op) {
-    if (FULL && op.y == OP_NOP) return;  // padding of a whole-update schedule
+  // PAD: the schedule holds OP_NOP padding (whole-update schedules only);
+  // the test is compiled in only for those, as it costs the others ~3 %
+  auto run = [&](uint2 op, auto pad) {
+    if constexpr (FULL && decltype(pad)::value) {
+      if (op.y == OP_NOP) return;
+    }
     if (FULL && op.y == OP_INTEG) {
       float2 p, q;
       if (SMEM) {
@@ -448,7 +452,7 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   //   before the barrier, so after it a thread's first load is its op.
   // A shared-memory prefetch of the next op ahead of the barrier measured
   // slower.
-  auto run_chunk = [&](uint32_t buf_a, auto one, auto kind) {
+  auto run_chunk = [&](uint32_t buf_a, auto one, auto kind, auto pad) {
     constexpr bool ONE = decltype(one)::value;
     constexpr int KIND = decltype(kind)::value;
     const uint32_t nseg = lds_u32(buf_a);
@@ -461,9 +465,9 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
       uint32_t end = __shfl_sync(0xFFFFFFFFu, my_end, 0);
       for (uint32_t j = 0; j < n; ++j) {
         if constexpr (ONE) {
-          if (beg + t < end) run(lds_u32x2(ops_a + 8u * (beg + t)));
+          if (beg + t < end) run(lds_u32x2(ops_a + 8u * (beg + t)), pad);
         } else {
-          for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k));
+          for (uint32_t k = beg + t; k < end; k += T) run(lds_u32x2(ops_a + 8u * k), pad);
         }
         const uint32_t next = __shfl_sync(0xFFFFFFFFu, my_end, (j + 1u) & 31u);
         if constexpr (KIND == 0) {
@@ -481,18 +485,24 @@ __global__ void k_exec_groups(const DWorld* __restrict__ worlds, DScheds SC,
   };
   const bool one = S.maxw <= T;
   const int kind = T == 32 ? 0 : (T == blockDim.x ? 1 : 2);  // as group_sync
-  auto walk = [&](uint32_t buf_a) {
+  auto walk_pad = [&](uint32_t buf_a, auto pad) {
     using I0 = std::integral_constant<int, 0>;
     using I1 = std::integral_constant<int, 1>;
     using I2 = std::integral_constant<int, 2>;
     if (one) {
-      return kind == 1 ? run_chunk(buf_a, std::true_type{}, I1{})
-             : kind == 0 ? run_chunk(buf_a, std::true_type{}, I0{})
-                         : run_chunk(buf_a, std::true_type{}, I2{});
+      return kind == 1 ? run_chunk(buf_a, std::true_type{}, I1{}, pad)
+             : kind == 0 ? run_chunk(buf_a, std::true_type{}, I0{}, pad)
+                         : run_chunk(buf_a, std::true_type{}, I2{}, pad);
     }
-    return kind == 1 ? run_chunk(buf_a, std::false_type{}, I1{})
-           : kind == 0 ? run_chunk(buf_a, std::false_type{}, I0{})
-                       : run_chunk(buf_a, std::false_type{}, I2{});
+    return kind == 1 ? run_chunk(buf_a, std::false_type{}, I1{}, pad)
+           : kind == 0 ? run_chunk(buf_a, std::false_type{}, I0{}, pad)
+                       : run_chunk(buf_a, std::false_type{}, I2{}, pad);
+  };
+  auto walk = [&](uint32_t buf_a) {
+    if constexpr (FULL) {
+      if (S.nop_pad) return walk_pad(buf_a, std::true_type{});
+    }
+    return walk_pad(buf_a, std::false_type{});
   };
 
   const uint32_t cbuf_a = smem_addr(cbuf);

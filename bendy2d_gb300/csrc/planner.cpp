@@ -96,18 +96,23 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
     std::vector<uint32_t> fill(start.begin(), start.end());
     for (size_t i = 0; i < total; ++i) sorted[fill[lvl_of[i]]++] = op_of[i];
   }
-  // Whole-update schedules: within each level the link solves first, then
-  // the bounds+integrate ops, the links padded with OP_NOP entries to a
-  // whole number of warps (a level's ops are independent, so this order
-  // gives the same results).  A warp then runs one kind only.  Padding
+  // Whole-update schedules whose levels fit one op per thread of a group of
+  // up to 512: within each level the link solves first, then the
+  // bounds+integrate ops, the links padded with OP_NOP entries to a whole
+  // number of warps (a level's ops are independent, so this order gives the
+  // same results).  A warp then runs one kind only (configuration 1 in
+  // reference order: 378 of 413 levels had a warp running both).  Padding
   // stays within the power of two above the widest level, so a group that
-  // ran every level with one op per thread still does.
+  // ran every level with one op per thread still does.  Wider schedules
+  // (fast order: levels of up to ~930 ops, several per thread, and hardly
+  // any mixed warps) keep their order.
   constexpr uint32_t NOP_ID = 0xFFFFFFFFu;
-  if (full) {
-    uint32_t maxw0 = 0;
-    for (uint32_t l = 1; l <= maxl; ++l) maxw0 = std::max(maxw0, start[l + 1] - start[l]);
-    uint32_t cap = 1;
-    while (cap < maxw0) cap <<= 1;
+  bool padded = false;
+  uint32_t maxw0 = 0;
+  for (uint32_t l = 1; l <= maxl; ++l) maxw0 = std::max(maxw0, start[l + 1] - start[l]);
+  uint32_t cap = 1;
+  while (cap < maxw0) cap <<= 1;
+  if (full && cap <= 512u) {
     std::vector<uint32_t> out, nstart(maxl + 2, 0);
     out.reserve(total + 32 * (size_t)maxl);
     for (uint32_t l = 1; l <= maxl; ++l) {
@@ -121,7 +126,10 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
         }
       const uint32_t ninteg = (e - b) - nlink;
       const uint32_t pad = (32u - nlink % 32u) % 32u;
-      if (nlink && ninteg && pad && nlink + pad + ninteg <= cap) out.insert(out.end(), pad, NOP_ID);
+      if (nlink && ninteg && pad && nlink + pad + ninteg <= cap) {
+        out.insert(out.end(), pad, NOP_ID);
+        padded = true;
+      }
       for (uint32_t i = b; i < e; ++i)
         if (sorted[i] & OP_INTEG) out.push_back(sorted[i]);
     }
@@ -190,6 +198,7 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   flush();
   d.nchunks = (uint32_t)chunk_off.size() - d.chunk0;
   d.off = d.words = d.len0 = d.maxw = 0;
+  d.nop_pad = padded ? 1u : 0u;
   for (uint32_t l = 1; l <= maxl; ++l) d.maxw = std::max(d.maxw, start[l + 1] - start[l]);
   if (d.nchunks) {
     d.off = chunk_off[d.chunk0];
