@@ -62,7 +62,11 @@ struct SchedRegistry {
   std::vector<DSched> scheds;
   std::vector<uint32_t> chunk_off, chunk_len, stream;
   size_t uploaded_scheds = 0, uploaded_chunks = 0, uploaded_stream = 0;
-  uint32_t get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I, bool full);
+  // wide: the schedule is for the large-body executor, which runs levels
+  // wider than a group (several ops per thread): whole-update schedules are
+  // grouped by op kind there whatever their width
+  uint32_t get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I, bool full,
+               bool wide = false);
 };
 
 struct GroupBody {

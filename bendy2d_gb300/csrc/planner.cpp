@@ -50,10 +50,10 @@ bool PlanTuning::set(const std::string& k, double v) {
 }
 
 uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32_t S, uint32_t I,
-                            bool full) {
+                            bool full, bool wide) {
   std::string key;
   key.resize(20 + (size_t)nl * 8);
-  const uint32_t hdr[5] = {np, nl, S, I, full ? 1u : 0u};
+  const uint32_t hdr[5] = {np, nl, S, I, (full ? 1u : 0u) | (full && wide ? 2u : 0u)};
   std::memcpy(&key[0], hdr, 20);
   if (nl) std::memcpy(&key[20], links, (size_t)nl * 8);
   auto it = index.find(key);
@@ -112,7 +112,7 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
   for (uint32_t l = 1; l <= maxl; ++l) maxw0 = std::max(maxw0, start[l + 1] - start[l]);
   uint32_t cap = 1;
   while (cap < maxw0) cap <<= 1;
-  if (full && cap <= 512u) {
+  if (full && (cap <= 512u || wide)) {
     std::vector<uint32_t> out, nstart(maxl + 2, 0);
     out.reserve(total + 32 * (size_t)maxl);
     for (uint32_t l = 1; l <= maxl; ++l) {
@@ -126,7 +126,7 @@ uint32_t SchedRegistry::get(const uint2* links, uint32_t nl, uint32_t np, uint32
         }
       const uint32_t ninteg = (e - b) - nlink;
       const uint32_t pad = (32u - nlink % 32u) % 32u;
-      if (nlink && ninteg && pad && nlink + pad + ninteg <= cap) {
+      if (nlink && ninteg && pad && (wide || nlink + pad + ninteg <= cap)) {
         out.insert(out.end(), pad, NOP_ID);
         padded = true;
       }
@@ -406,13 +406,17 @@ int plan_world(const WorldHost& w, const PlanTuning& tune, SchedRegistry& reg, W
         im.lstiff.push_back(L.stiffness);
       }
     B.nl = (uint32_t)loc.size();
-    B.sched = reg.get(loc.data(), B.nl, B.np, P.S, P.I, full);
+    const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 8u * (size_t)B.nl);
+    const bool smem = region <= tune.smem_max && B.np <= 65535u;
+    // whether the large-body executor (below) will run it
+    const bool to_large = !smem && tune.large_max > 0 && B.np > 0 &&
+                          (B.np + (1u << (full ? 13u : 14u)) - 1u) >> (full ? 13u : 14u) <=
+                              tune.large_max;
+    B.sched = reg.get(loc.data(), B.nl, B.np, P.S, P.I, full, to_large);
     const DSched& S = reg.scheds[B.sched];
     const float avg = S.nlvl ? (float)S.nops / (float)S.nlvl : 1.0f;
     uint32_t T = pow2ceil((uint32_t)(avg / tune.width_per_thread + 0.999f));
     T = std::min(std::max(T, tune.t_min), tune.t_max);
-    const size_t region = align16((full ? 16u : 8u) * (size_t)B.np + 8u * (size_t)B.nl);
-    const bool smem = region <= tune.smem_max && B.np <= 65535u;
     // the whole schedule resident in shared memory when it fits beside the body
     uint32_t res = 0;
     if (smem && tune.resident) {
